@@ -1,0 +1,393 @@
+"""Multisplit benchmark on GB300.
+
+Default workload (one step = one stable key-value multisplit):
+    2^28 (uint32 key, uint32 value) pairs, values = original index, keys uniform
+    over [0, 2^32) (splitmix64, seed 3), 256 buckets by delta bucketing
+    (bucket = key * 256 >> 32).
+Inputs (2 GiB) and outputs (2 GiB) are far larger than the 129 MB L2, so no
+flush is needed between steps.
+
+`value` is whole-job Gkeys/s (one key-value pair = one key) with inputs resident
+in HBM; the step runs prescan, scan and postscan through the C ABI's stage
+entry points with CUDA events between them, which also yields the postscan's
+own duration for the roofline.  `e2e` is the same metric through the one-call
+public API with pinned host buffers: host->device copy of keys and values, the
+multisplit, and device->host copy of both outputs inside every timed step.
+
+--impl reference times the CPU implementation of the same path (the oracle's
+multi-threaded restatement of the reference's cpu_multisplit_pairs_general,
+oracle/oracle.c) on the host cores.
+
+Multi-GPU (torchrun): every rank runs its own replica of the workload (weak
+scaling, no collective on the data path); timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gkeys/s & %HBM roofline at 2^28 keys; batched-vs-plain Gkeys/s, p50/p99 lat"
+UNIT = "Gkeys/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--log2n", type=int, default=28)
+    p.add_argument("--buckets", type=int, default=256)
+    p.add_argument("--dist", default="uniform", choices=["uniform", "zipf"])
+    p.add_argument("--identifier", default="delta", choices=["delta", "range"])
+    p.add_argument("--keys-only", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline time budget")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_config(a):
+    n = 1 << a.log2n
+    return {
+        "workload": f"{'key-only' if a.keys_only else 'key-value'} stable multisplit, 2^{a.log2n} "
+                    f"{'keys' if a.keys_only else 'pairs (values = index)'}, {a.buckets} buckets, "
+                    f"{a.identifier} identifier, {a.dist} uint32 keys",
+        "n": n,
+        "buckets": a.buckets,
+        "identifier": "delta (key*B>>32)" if a.identifier == "delta" else "range (B sorted splitters, s[0]=0)",
+        "distribution": a.dist if a.dist == "uniform" else "zipf s=1.1 over 2^20 distinct keys",
+        "key_value": not a.keys_only,
+        "l2": "inputs larger than L2 (no flush needed)",
+    }
+
+
+def algorithmic_bytes(a):
+    # prescan reads keys (4 B); postscan reads keys (+values) and writes them.
+    per_key_step = 12 if a.keys_only else 20
+    per_key_post = 8 if a.keys_only else 16
+    return per_key_step, per_key_post
+
+
+def make_inputs(a, device):
+    from gpumultisplit_gb300 import datagen
+
+    n = 1 << a.log2n
+    keys = (datagen.uniform_u32 if a.dist == "uniform" else datagen.zipf_u32)(n, 3, device=device)
+    vals = None if a.keys_only else datagen.index_values(n, device)
+    spl = datagen.range_splitters(a.buckets, 5, device) if a.identifier == "range" else None
+    return keys, vals, spl
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(prefix="gms_clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        pw = [num(r[3]) for r in rows if num(r[3]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None, "samples": len(rows), "reasons": reasons}
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str, n: int):
+    """Per-launch DRAM bytes of `kernel` from a committed ncu capture summary,
+    scaled to n keys (profiles/traffic.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            rec = json.load(f)[kernel]
+        return rec["dram_bytes_per_key"] * n
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def cpu_baseline(a, keys_dev, vals_dev, seconds):
+    """Times the oracle's multi-threaded restatement on a bounded sample."""
+    import oracle
+    from gpumultisplit_gb300 import datagen
+
+    threads = os.cpu_count() or 1
+    n = keys_dev.numel()
+    keys = datagen.as_u32(keys_dev)
+    vals = None if vals_dev is None else datagen.as_u32(vals_dev)
+    spl = None
+    if a.identifier == "range":
+        spl = datagen.as_u32(datagen.range_splitters(a.buckets, 5))
+    d = oracle.Desc(oracle.DELTA if a.identifier == "delta" else oracle.RANGE, a.buckets, splitters=spl)
+    oracle.multisplit_mt(keys[: 1 << 20], d, None if vals is None else vals[: 1 << 20], threads)  # warm
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        oracle.multisplit_mt(keys, d, vals, threads)
+        reps += 1
+        if time.perf_counter() - t0 >= seconds or reps >= 50:
+            break
+    el = time.perf_counter() - t0
+    return {"value": reps * n / el / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reps} full multisplits of the same 2^{a.log2n}-key workload, "
+                      f"{threads} threads (oracle/oracle.c oracle_multisplit_mt), {el:.1f} s"}
+
+
+def run_reference(a):
+    """--impl reference: the CPU implementation of the path on the host cores."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    from gpumultisplit_gb300 import datagen
+
+    if not oracle.LIB.exists():
+        oracle.build(with_ref=False)
+    n = 1 << a.log2n
+    keys_t, vals_t, spl_t = make_inputs(a, "cpu")
+    keys = datagen.as_u32(keys_t)
+    vals = None if vals_t is None else datagen.as_u32(vals_t)
+    spl = None if spl_t is None else datagen.as_u32(spl_t)
+    d = oracle.Desc(oracle.DELTA if a.identifier == "delta" else oracle.RANGE, a.buckets, splitters=spl)
+    threads = os.cpu_count() or 1
+    for _ in range(a.warmup):
+        oracle.multisplit_mt(keys, d, vals, threads)
+    times = []
+    for _ in range(a.steps):
+        t0 = time.perf_counter()
+        oracle.multisplit_mt(keys, d, vals, threads)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = a.steps * n / tot / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * tot / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic", "config": workload_config(a),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"full 2^{a.log2n}-key workload per step, {threads} threads "
+                                   "(oracle/oracle.c oracle_multisplit_mt: the reference's "
+                                   "cpu_multisplit_pairs_general algorithm, chunked across threads)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(a):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    import gpumultisplit_gb300 as gms
+    from gpumultisplit_gb300 import build as gbuild
+
+    gbuild.build()
+    gms.load()
+
+    n = 1 << a.log2n
+    B = a.buckets
+    keys, vals, spl = make_inputs(a, dev)
+    kout = torch.empty_like(keys)
+    vout = None if vals is None else torch.empty_like(vals)
+    ident = gms.delta_bucket() if a.identifier == "delta" else gms.range_bucket(spl)
+    ctx = gms.multisplit_context(B)
+    (gms.multisplit_allocate_key_only if a.keys_only else gms.multisplit_allocate_key_value)(n, ctx)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    def step(ev=None):
+        gms.multisplit_stages(keys, vals, kout, vout, n, ctx, ident, events=ev)
+
+    for _ in range(max(3, a.warmup)):
+        step()
+    torch.cuda.synchronize()
+    assert gms.read_device_error(ctx) == 0
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(a.steps)]
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        for i in range(a.steps):
+            step(evs[i])
+        torch.cuda.synchronize()
+        barrier()
+    clocks = clk.summary()
+    assert gms.read_device_error(ctx) == 0
+    total_ms = evs[0][0].elapsed_time(evs[-1][3])
+    pre = [e[0].elapsed_time(e[1]) for e in evs]
+    scan = [e[1].elapsed_time(e[2]) for e in evs]
+    post = [e[2].elapsed_time(e[3]) for e in evs]
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / a.steps
+    value = world * n / (ms_per_step * 1e-3) / 1e9
+
+    # End to end through the one-call public API, host buffers, copies inside the step.
+    e2e = None
+    if not a.no_e2e:
+        hk = torch.empty(n, dtype=torch.int32, pin_memory=True)
+        hk.copy_(keys)
+        hv = torch.empty(n, dtype=torch.int32, pin_memory=True) if vals is not None else None
+        if hv is not None:
+            hv.copy_(vals)
+        hko = torch.empty(n, dtype=torch.int32, pin_memory=True)
+        hvo = torch.empty(n, dtype=torch.int32, pin_memory=True) if vals is not None else None
+        dk, dv = torch.empty_like(keys), (torch.empty_like(vals) if vals is not None else None)
+
+        def e2e_step():
+            dk.copy_(hk, non_blocking=True)
+            if dv is not None:
+                dv.copy_(hv, non_blocking=True)
+            if dv is None:
+                gms.multisplit_key_only(dk, kout, n, ctx, ident)
+            else:
+                gms.multisplit_key_value(dk, dv, kout, vout, n, ctx, ident)
+            hko.copy_(kout, non_blocking=True)
+            if hvo is not None:
+                hvo.copy_(vout, non_blocking=True)
+
+        for _ in range(max(3, a.warmup)):
+            e2e_step()
+        torch.cuda.synchronize()
+        e_steps = max(3, a.steps // 2)
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        s0.record()
+        for _ in range(e_steps):
+            e2e_step()
+        s1.record()
+        torch.cuda.synchronize()
+        barrier()
+        e_ms = s0.elapsed_time(s1) / e_steps
+        if world > 1:
+            import torch.distributed as dist
+
+            t = torch.tensor([e_ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_ms = float(t.item())
+        nb = n * 4 * (1 if vals is None else 2)
+        e2e = {"value": world * n / (e_ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": e_ms,
+               "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb}
+        # the e2e output must be the same multisplit
+        assert torch.equal(hko, kout.cpu())
+
+    per_key_step, per_key_post = algorithmic_bytes(a)
+    peak, peak_src = hbm_peak()
+    post_ms = statistics.mean(post)
+    achieved = per_key_post * n / (post_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "postscan_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": per_key_post * n,
+                "traffic": ncu_traffic("postscan_kv" if vals is not None else "postscan_k", n)}
+    step_gbs = per_key_step * n / (ms_per_step * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic", "config": workload_config(a),
+        "roofline": roofline,
+        "step_roofline": {"achieved": step_gbs, "frac": step_gbs / peak, "unit": "GB/s",
+                          "algorithmic_bytes_per_key": per_key_step},
+        "stages_ms": {"prescan": statistics.mean(pre), "scan": statistics.mean(scan), "postscan": post_ms},
+        "clocks": clocks, "gpu_launches": 3 * a.steps, "e2e": e2e,
+    }
+    if rank == 0 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(a, keys, vals, a.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

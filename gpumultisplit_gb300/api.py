@@ -1,0 +1,423 @@
+"""Host-side mirror of the reference's multisplit API, on the C ABI.
+
+Names, argument order and meaning follow the reference headers:
+  * multisplit_context / multisplit_allocate_key_only / _key_value /
+    multisplit_release_memory / multisplit_key_only / multisplit_key_value
+    (src/api/multisplit.cuh:29-313);
+  * ms_sort_context / multisplit_sort_7bit_allocate / _allocate_pairs /
+    multisplit_sort_7bit / multisplit_sort_7bit_pairs / multisplit_sort_release_memory
+    (src/api/multisplit_sort.cuh:100-364, src/api/multisplit_sort_pairs.cuh:21-65);
+  * compaction_context / compaction_allocate_key_only / _key_value /
+    compaction_release_memory / compaction_key_only / compaction_key_value
+    (src/kernels/compaction/multisplit2_compaction.cuh:477-573);
+  * histogram_even / histogram_range: the launches of the reference's histogram
+    kernels (src/main/main_histogram.cu:163-179, 272-279), plus
+    multisplit_histogram for any identifier.
+
+Device buffers are CUDA torch tensors of a 4-byte dtype (int32 or uint32) or raw
+device addresses (int).  Calls run on torch's current CUDA stream.
+
+Error behaviour: the reference's functions return void and print on an
+unsupported bucket count (src/api/multisplit.cuh:135-136); these raise GmsError
+instead, so a failed call is never silent.
+
+Bucket identifiers: the reference passes a functor; a precompiled library takes
+a descriptor.  The identifier classes below cover the functors the reference and
+its drivers use (delta_func, ms_bucket_sort_*bit, test_bucket) and the
+identifiers of the benchmark configurations (delta key*B>>32, range splitters).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+from . import _lib
+from ._lib import BucketDesc, check
+
+# ---------------------------------------------------------------- helpers
+
+
+def _ptr(x) -> int | None:
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if x.element_size() != 4:
+            raise TypeError("multisplit buffers hold 32-bit elements")
+        if not x.is_cuda:
+            raise TypeError("multisplit buffers must be CUDA tensors")
+        return x.data_ptr()
+    raise TypeError(f"unsupported buffer type {type(x)!r}")
+
+
+def _stream(stream=None) -> int | None:
+    if stream is not None:
+        return stream if isinstance(stream, int) else stream.cuda_stream
+    import torch
+
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _alloc_scratch(nbytes: int):
+    import torch
+
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device="cuda")
+
+
+# ------------------------------------------------------ bucket identifiers
+
+
+class BucketIdentifier:
+    """Base class: produces a gms_bucket_desc for a given bucket count."""
+
+    def desc(self, num_buckets: int) -> BucketDesc:  # pragma: no cover - abstract
+        raise NotImplementedError
+
+
+@dataclass
+class delta_bucket(BucketIdentifier):
+    """bucket = key * B >> 32 (B equal-width ranges of the 32-bit key space)."""
+
+    def desc(self, num_buckets):
+        return BucketDesc(kind=_lib.GMS_BUCKET_DELTA, num_buckets=num_buckets)
+
+
+@dataclass
+class delta_func(BucketIdentifier):
+    """bucket = key / delta (README.md:85-91, src/main/main_multisplit.cu:41-47)."""
+
+    delta: int
+
+    def desc(self, num_buckets):
+        return BucketDesc(kind=_lib.GMS_BUCKET_DIV, num_buckets=num_buckets, param=int(self.delta))
+
+
+@dataclass
+class bits_bucket(BucketIdentifier):
+    """bucket = (key >> shift) & (B - 1)."""
+
+    shift: int = 0
+
+    def desc(self, num_buckets):
+        return BucketDesc(kind=_lib.GMS_BUCKET_BITS, num_buckets=num_buckets, shift=int(self.shift))
+
+
+def ms_bucket_sort_4bit(shift: int) -> bits_bucket:
+    """ms_bucket_sort_4bit<shift> (src/api/multisplit_sort.cuh:63-68)."""
+    return bits_bucket(shift)
+
+
+def ms_bucket_sort_7bit(shift: int) -> bits_bucket:
+    """ms_bucket_sort_7bit<shift> (src/api/multisplit_sort.cuh:81-86)."""
+    return bits_bucket(shift)
+
+
+def test_bucket(flag: int = 1) -> BucketIdentifier:
+    """test_bucket<flag>: key & ((1 << flag) - 1) (src/main/main_compaction.cu:26-31)."""
+    if flag != 1:
+        raise ValueError("only test_bucket<1> (key & 1) is a two-bucket identifier")
+    return bits_bucket(0)
+
+
+@dataclass
+class mask_bucket(BucketIdentifier):
+    """bucket = (key & mask) != 0."""
+
+    mask: int
+
+    def desc(self, num_buckets):
+        return BucketDesc(kind=_lib.GMS_BUCKET_MASK, num_buckets=num_buckets, param=int(self.mask))
+
+
+class range_bucket(BucketIdentifier):
+    """bucket = upper_bound(splitters, key) - 1 over B sorted splitters (device
+    tensor), the level search of src/kernels/histogram/multisplit2_histograms.cuh:434."""
+
+    def __init__(self, d_splitters):
+        self.d_splitters = d_splitters
+
+    def desc(self, num_buckets):
+        return BucketDesc(kind=_lib.GMS_BUCKET_RANGE, num_buckets=num_buckets, d_splitters=_ptr(self.d_splitters))
+
+
+@dataclass
+class even_float_bucket(BucketIdentifier):
+    """bin = (uint32)((key - lower) * inverse_delta) in float arithmetic
+    (src/kernels/histogram/multisplit2_histograms.cuh:60)."""
+
+    lower: int
+    inverse_delta: float
+
+    def desc(self, num_buckets):
+        return BucketDesc(kind=_lib.GMS_BUCKET_EVEN_FLOAT, num_buckets=num_buckets, lower=int(self.lower),
+                          inverse_delta=float(self.inverse_delta))
+
+
+# -------------------------------------------------------------- multisplit
+
+
+class multisplit_context:
+    """multisplit_context (src/api/multisplit.cuh:29-47)."""
+
+    def __init__(self, n_buckets: int):
+        self.num_buckets = int(n_buckets)
+        self.size_sub_prob = 0
+        self.num_sub_prob = 0
+        self.num_blocks = 0
+        self.d_temp_storage = None
+        self.temp_storage_bytes = 0
+        self.key_value = False
+        self.capacity = 0
+
+    @property
+    def d_histogram(self):
+        """Bucket-major count matrix inside the scratch, laid out for num_elements =
+        the allocated capacity (after a call: global offsets, offset(b, tile) at
+        [b * num_sub_prob + tile]).  It always starts 256 bytes into the scratch."""
+        if self.d_temp_storage is None:
+            return None
+        import torch
+
+        off = ctypes.c_size_t()
+        check(_lib.load().gms_multisplit_geometry(self.capacity, self.num_buckets, int(self.key_value), None, None,
+                                                  ctypes.byref(off)), "multisplit_geometry")
+        return self.d_temp_storage[off.value:off.value + 4 * self.num_buckets * self.num_sub_prob].view(torch.int32)
+
+
+def _ms_allocate(num_elements: int, context: multisplit_context, key_value: bool) -> None:
+    lib = _lib.load()
+    nbytes = ctypes.c_size_t()
+    check(lib.gms_multisplit_scratch_bytes(num_elements, context.num_buckets, int(key_value), ctypes.byref(nbytes)),
+          "multisplit_allocate")
+    tile, tiles = ctypes.c_uint32(), ctypes.c_uint32()
+    check(lib.gms_multisplit_geometry(num_elements, context.num_buckets, int(key_value), ctypes.byref(tile),
+                                      ctypes.byref(tiles), None), "multisplit_geometry")
+    context.size_sub_prob = tile.value
+    context.num_sub_prob = tiles.value
+    context.num_blocks = tiles.value
+    context.temp_storage_bytes = nbytes.value
+    context.d_temp_storage = _alloc_scratch(nbytes.value)
+    context.key_value = key_value
+    context.capacity = int(num_elements)
+
+
+def multisplit_allocate_key_only(num_elements: int, context: multisplit_context) -> None:
+    """src/api/multisplit.cuh:50-61."""
+    _ms_allocate(num_elements, context, False)
+
+
+def multisplit_allocate_key_value(num_elements: int, context: multisplit_context) -> None:
+    """src/api/multisplit.cuh:63-74."""
+    _ms_allocate(num_elements, context, True)
+
+
+def multisplit_release_memory(context: multisplit_context) -> None:
+    """src/api/multisplit.cuh:76-79."""
+    context.d_temp_storage = None
+    context.temp_storage_bytes = 0
+
+
+def _offsets_buffer(num_buckets):
+    return (ctypes.c_uint32 * num_buckets)()
+
+
+def multisplit_key_only(d_key_in, d_key_out, num_elements: int, context: multisplit_context,
+                        bucket_identifier: BucketIdentifier, multisplit_offset=None, stream=None):
+    """src/api/multisplit.cuh:81-197.  If multisplit_offset is a list (or True),
+    the B bucket start offsets are returned (and written into a given list)."""
+    desc = bucket_identifier.desc(context.num_buckets)
+    offs = _offsets_buffer(context.num_buckets) if multisplit_offset is not None else None
+    check(_lib.load().gms_multisplit_key_only(_ptr(d_key_in), _ptr(d_key_out), num_elements, ctypes.byref(desc),
+                                              _ptr(context.d_temp_storage), context.temp_storage_bytes, offs,
+                                              _stream(stream)), "multisplit_key_only")
+    return _export_offsets(offs, multisplit_offset)
+
+
+def multisplit_key_value(d_key_in, d_value_in, d_key_out, d_value_out, num_elements: int,
+                         context: multisplit_context, bucket_identifier: BucketIdentifier, multisplit_offset=None,
+                         stream=None):
+    """src/api/multisplit.cuh:199-313."""
+    desc = bucket_identifier.desc(context.num_buckets)
+    offs = _offsets_buffer(context.num_buckets) if multisplit_offset is not None else None
+    check(_lib.load().gms_multisplit_key_value(_ptr(d_key_in), _ptr(d_value_in), _ptr(d_key_out), _ptr(d_value_out),
+                                               num_elements, ctypes.byref(desc), _ptr(context.d_temp_storage),
+                                               context.temp_storage_bytes, offs, _stream(stream)),
+          "multisplit_key_value")
+    return _export_offsets(offs, multisplit_offset)
+
+
+def _export_offsets(offs, target):
+    if offs is None:
+        return None
+    vals = list(offs)
+    if isinstance(target, list):
+        target[:] = vals
+    return vals
+
+
+def multisplit_stages(d_key_in, d_value_in, d_key_out, d_value_out, num_elements: int,
+                      context: multisplit_context, bucket_identifier: BucketIdentifier, stream=None,
+                      events=None):
+    """Runs prescan, scan and postscan as three C-ABI calls (same result as
+    multisplit_key_only / _key_value).  If `events` holds four CUDA events they
+    are recorded before, between and after the stages."""
+    lib = _lib.load()
+    desc = bucket_identifier.desc(context.num_buckets)
+    kv = int(d_value_in is not None)
+    s = _stream(stream)
+    scratch, nbytes = _ptr(context.d_temp_storage), context.temp_storage_bytes
+    if events:
+        events[0].record()
+    check(lib.gms_multisplit_prescan(_ptr(d_key_in), num_elements, ctypes.byref(desc), kv, scratch, nbytes, s),
+          "multisplit_prescan")
+    if events:
+        events[1].record()
+    check(lib.gms_multisplit_scan(num_elements, ctypes.byref(desc), kv, scratch, nbytes, s), "multisplit_scan")
+    if events:
+        events[2].record()
+    check(lib.gms_multisplit_postscan(_ptr(d_key_in), _ptr(d_value_in), _ptr(d_key_out), _ptr(d_value_out),
+                                      num_elements, ctypes.byref(desc), scratch, nbytes, s), "multisplit_postscan")
+    if events:
+        events[3].record()
+
+
+def read_device_error(context, stream=None) -> int:
+    """Device error word of a context's scratch (0 = every bounded wait finished)."""
+    code = ctypes.c_uint32()
+    st = _lib.load().gms_read_device_error(_ptr(context.d_temp_storage), ctypes.byref(code), _stream(stream))
+    if st not in (_lib.GMS_SUCCESS, _lib.GMS_ERROR_DEVICE_TIMEOUT):
+        check(st, "read_device_error")
+    return code.value
+
+
+# -------------------------------------------------------------------- sort
+
+
+class ms_sort_context:
+    """ms_sort_context (src/api/multisplit_sort.cuh:100-116)."""
+
+    def __init__(self):
+        self.d_temp_storage = None
+        self.temp_storage_bytes = 0
+
+
+def _sort_allocate(n_elements, context, key_value):
+    nbytes = ctypes.c_size_t()
+    check(_lib.load().gms_sort_7bit_scratch_bytes(n_elements, int(key_value), ctypes.byref(nbytes)),
+          "multisplit_sort_7bit_allocate")
+    context.temp_storage_bytes = nbytes.value
+    context.d_temp_storage = _alloc_scratch(nbytes.value)
+
+
+def multisplit_sort_7bit_allocate(n_elements: int, context: ms_sort_context) -> None:
+    """src/api/multisplit_sort.cuh:151-170."""
+    _sort_allocate(n_elements, context, False)
+
+
+def multisplit_sort_7bit_allocate_pairs(n_elements: int, context: ms_sort_context) -> None:
+    """src/api/multisplit_sort.cuh:171-191."""
+    _sort_allocate(n_elements, context, True)
+
+
+def multisplit_sort_release_memory(context: ms_sort_context) -> None:
+    """src/api/multisplit_sort.cuh:312-318."""
+    context.d_temp_storage = None
+    context.temp_storage_bytes = 0
+
+
+def multisplit_sort_7bit(d_key_in, d_key_out_ms, n_elements: int, context: ms_sort_context, stream=None) -> None:
+    """src/api/multisplit_sort.cuh:320-364."""
+    check(_lib.load().gms_sort_7bit_key_only(_ptr(d_key_in), _ptr(d_key_out_ms), n_elements,
+                                             _ptr(context.d_temp_storage), context.temp_storage_bytes,
+                                             _stream(stream)), "multisplit_sort_7bit")
+
+
+def multisplit_sort_7bit_pairs(d_key_in, d_key_out_ms, d_value_in, d_value_out_ms, n_elements: int,
+                               context: ms_sort_context, stream=None) -> None:
+    """src/api/multisplit_sort_pairs.cuh:21-65 (argument order kin, kout, vin, vout)."""
+    check(_lib.load().gms_sort_7bit_key_value(_ptr(d_key_in), _ptr(d_key_out_ms), _ptr(d_value_in),
+                                              _ptr(d_value_out_ms), n_elements, _ptr(context.d_temp_storage),
+                                              context.temp_storage_bytes, _stream(stream)),
+          "multisplit_sort_7bit_pairs")
+
+
+# -------------------------------------------------------------- compaction
+
+
+class compaction_context:
+    """compaction_context (src/kernels/compaction/multisplit2_compaction.cuh:477-489)."""
+
+    def __init__(self):
+        self.d_temp_storage = None
+        self.temp_storage_bytes = 0
+
+
+def _compaction_allocate(n, context, key_value):
+    nbytes = ctypes.c_size_t()
+    check(_lib.load().gms_compaction_scratch_bytes(n, int(key_value), ctypes.byref(nbytes)), "compaction_allocate")
+    context.temp_storage_bytes = nbytes.value
+    context.d_temp_storage = _alloc_scratch(nbytes.value)
+
+
+def compaction_allocate_key_only(num_elements: int, context: compaction_context) -> None:
+    """multisplit2_compaction.cuh:491-503."""
+    _compaction_allocate(num_elements, context, False)
+
+
+def compaction_allocate_key_value(num_elements: int, context: compaction_context) -> None:
+    """multisplit2_compaction.cuh:505-517."""
+    _compaction_allocate(num_elements, context, True)
+
+
+def compaction_release_memory(context: compaction_context) -> None:
+    """multisplit2_compaction.cuh:519-523."""
+    context.d_temp_storage = None
+    context.temp_storage_bytes = 0
+
+
+def compaction_key_only(d_key_in, d_key_out, num_elements: int, context: compaction_context,
+                        bucket_identifier: BucketIdentifier, stream=None) -> int:
+    """multisplit2_compaction.cuh:525-548; returns the number of bucket-0 keys."""
+    desc = bucket_identifier.desc(2)
+    n0 = ctypes.c_uint32()
+    check(_lib.load().gms_compaction_key_only(_ptr(d_key_in), _ptr(d_key_out), num_elements, ctypes.byref(desc),
+                                              _ptr(context.d_temp_storage), context.temp_storage_bytes,
+                                              ctypes.byref(n0), _stream(stream)), "compaction_key_only")
+    return n0.value
+
+
+def compaction_key_value(d_key_in, d_value_in, d_key_out, d_value_out, num_elements: int,
+                         context: compaction_context, bucket_identifier: BucketIdentifier, stream=None) -> int:
+    """multisplit2_compaction.cuh:550-573; returns the number of bucket-0 keys."""
+    desc = bucket_identifier.desc(2)
+    n0 = ctypes.c_uint32()
+    check(_lib.load().gms_compaction_key_value(_ptr(d_key_in), _ptr(d_value_in), _ptr(d_key_out), _ptr(d_value_out),
+                                               num_elements, ctypes.byref(desc), _ptr(context.d_temp_storage),
+                                               context.temp_storage_bytes, ctypes.byref(n0), _stream(stream)),
+          "compaction_key_value")
+    return n0.value
+
+
+# --------------------------------------------------------------- histogram
+
+
+def multisplit_histogram(d_key_in, num_elements: int, d_histogram, num_buckets: int,
+                         bucket_identifier: BucketIdentifier, stream=None) -> None:
+    """Adds per-bucket counts into d_histogram[0..B) (int32, zeroed by the caller)."""
+    desc = bucket_identifier.desc(num_buckets)
+    check(_lib.load().gms_histogram(_ptr(d_key_in), num_elements, ctypes.byref(desc), _ptr(d_histogram),
+                                    _stream(stream)), "multisplit_histogram")
+
+
+def histogram_even(d_key_in, num_elements: int, d_histogram, num_bins: int, lower_level: int, upper_level: int,
+                   inverse_delta: float, stream=None) -> None:
+    """multisplit2_histogram_even_* (src/kernels/histogram/multisplit2_histograms.cuh:36-400)."""
+    check(_lib.load().gms_histogram_even(_ptr(d_key_in), num_elements, _ptr(d_histogram), num_bins, lower_level,
+                                         upper_level, float(inverse_delta), _stream(stream)), "histogram_even")
+
+
+def histogram_range(d_key_in, num_elements: int, d_histogram, num_bins: int, d_levels, stream=None) -> None:
+    """multisplit2_histogram_range_* (src/kernels/histogram/multisplit2_histograms.cuh:403-699)."""
+    check(_lib.load().gms_histogram_range(_ptr(d_key_in), num_elements, _ptr(d_histogram), num_bins, _ptr(d_levels),
+                                          _stream(stream)), "histogram_range")

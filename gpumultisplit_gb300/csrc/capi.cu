@@ -1,0 +1,410 @@
+// The library's C ABI (include/gpumultisplit.h): argument checks, scratch
+// layout, stage orchestration, and the multi-pass operations built on the
+// multisplit (7-bit radix sort, two-bucket compaction).
+#include <atomic>
+#include <cstring>
+
+#include "../../include/gpumultisplit.h"
+#include "ms_host.h"
+#include "scan_kernels.cuh"
+
+namespace gms {
+
+namespace {
+thread_local int g_last_cuda_error = 0;
+
+gms_status cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return GMS_SUCCESS;
+  g_last_cuda_error = int(e);
+  return GMS_ERROR_CUDA;
+}
+
+bool valid_buckets(uint32_t b, int* logb) {
+  if (b < 2 || b > 256 || (b & (b - 1)) != 0) return false;
+  int l = 0;
+  while ((1u << l) < b) ++l;
+  *logb = l;
+  return true;
+}
+
+template <int LOGB, bool KV>
+constexpr uint32_t tile_of() {
+  return uint32_t(TileShape<LOGB, KV>::WARPS) * 32u * uint32_t(TileShape<LOGB, KV>::IPT);
+}
+
+gms_status check_desc(const gms_bucket_desc* d, int* logb) {
+  if (d == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (!valid_buckets(d->num_buckets, logb)) return GMS_ERROR_UNSUPPORTED_BUCKETS;
+  switch (d->kind) {
+    case GMS_BUCKET_DELTA:
+    case GMS_BUCKET_BITS:
+    case GMS_BUCKET_MASK:
+    case GMS_BUCKET_EVEN_FLOAT:
+      return GMS_SUCCESS;
+    case GMS_BUCKET_DIV:
+      return d->param != 0 ? GMS_SUCCESS : GMS_ERROR_INVALID_VALUE;
+    case GMS_BUCKET_RANGE:
+      return d->d_splitters != nullptr ? GMS_SUCCESS : GMS_ERROR_INVALID_VALUE;
+    default:
+      return GMS_ERROR_INVALID_VALUE;
+  }
+}
+
+BucketParams to_params(const gms_bucket_desc* d) {
+  BucketParams p;
+  p.shift = d->shift;
+  p.param = d->param;
+  p.lower = d->lower;
+  p.inverse_delta = d->inverse_delta;
+  p.splitters = d->d_splitters;
+  return p;
+}
+
+cudaError_t dispatch(int kind, const MsCall& c, int stages) {
+  switch (kind) {
+    case KIND_DELTA: return run_multisplit<KIND_DELTA>(c, stages);
+    case KIND_DIV: return run_multisplit<KIND_DIV>(c, stages);
+    case KIND_BITS: return run_multisplit<KIND_BITS>(c, stages);
+    case KIND_RANGE: return run_multisplit<KIND_RANGE>(c, stages);
+    case KIND_MASK: return run_multisplit<KIND_MASK>(c, stages);
+    case KIND_EVEN_FLOAT: return run_multisplit<KIND_EVEN_FLOAT>(c, stages);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t dispatch_hist(int kind, const uint32_t* keys, uint32_t n, int logb, const BucketParams& bp,
+                          int32_t* hist, cudaStream_t s) {
+  switch (kind) {
+    case KIND_DELTA: return run_histogram<KIND_DELTA>(keys, n, logb, bp, hist, s);
+    case KIND_DIV: return run_histogram<KIND_DIV>(keys, n, logb, bp, hist, s);
+    case KIND_BITS: return run_histogram<KIND_BITS>(keys, n, logb, bp, hist, s);
+    case KIND_RANGE: return run_histogram<KIND_RANGE>(keys, n, logb, bp, hist, s);
+    case KIND_MASK: return run_histogram<KIND_MASK>(keys, n, logb, bp, hist, s);
+    case KIND_EVEN_FLOAT: return run_histogram<KIND_EVEN_FLOAT>(keys, n, logb, bp, hist, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+bool overlaps(const void* a, const void* b, uint32_t n) {
+  if (a == nullptr || b == nullptr || n == 0) return false;
+  const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+  const uintptr_t len = uintptr_t(n) * 4u;
+  return x < y + len && y < x + len;
+}
+
+// Shared body of the multisplit entry points (stage mask selects the kernels).
+gms_status multisplit_impl(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n,
+                           const gms_bucket_desc* desc, bool kv, void* scratch, size_t scratch_bytes,
+                           int stages, cudaStream_t stream) {
+  int logb = 0;
+  gms_status st = check_desc(desc, &logb);
+  if (st != GMS_SUCCESS) return st;
+  if (n == 0) return GMS_SUCCESS;
+  if (scratch == nullptr || (reinterpret_cast<uintptr_t>(scratch) & 255u) != 0) return GMS_ERROR_INVALID_VALUE;
+  if ((stages & (STAGE_PRESCAN | STAGE_POSTSCAN)) && kin == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (stages & STAGE_POSTSCAN) {
+    if (kout == nullptr || overlaps(kin, kout, n)) return GMS_ERROR_INVALID_VALUE;
+    if (kv && (vin == nullptr || vout == nullptr || overlaps(vin, vout, n) || overlaps(kout, vout, n)))
+      return GMS_ERROR_INVALID_VALUE;
+  }
+  const Geometry g = make_geometry(n, logb, kv);
+  if (scratch_bytes < g.bytes) return GMS_ERROR_SCRATCH_TOO_SMALL;
+  MsCall c;
+  c.kin = kin;
+  c.vin = vin;
+  c.kout = kout;
+  c.vout = vout;
+  c.n = n;
+  c.logb = logb;
+  c.kv = kv;
+  c.bp = to_params(desc);
+  c.scratch = static_cast<unsigned char*>(scratch);
+  c.stream = stream;
+  return cuda_status(dispatch(desc->kind, c, stages));
+}
+
+// Bucket start offsets: matrix[b * num_tiles] for every b (src/api/multisplit.cuh:143-149).
+gms_status copy_offsets(const void* scratch, uint32_t n, int logb, bool kv, uint32_t* h_offsets,
+                        cudaStream_t stream) {
+  const uint32_t B = 1u << logb;
+  if (n == 0) {
+    for (uint32_t b = 0; b < B; ++b) h_offsets[b] = 0;
+    return GMS_SUCCESS;
+  }
+  const Geometry g = make_geometry(n, logb, kv);
+  const auto* matrix = static_cast<const unsigned char*>(scratch) + g.off_matrix;
+  cudaError_t e = cudaMemcpy2DAsync(h_offsets, sizeof(uint32_t), matrix, size_t(g.num_tiles) * 4, sizeof(uint32_t),
+                                    B, cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  return cuda_status(e);
+}
+
+struct SortLayout {
+  size_t ms_bytes;   // multisplit scratch (largest of the two digit widths)
+  size_t off_keys;   // ping-pong keys
+  size_t off_vals;   // ping-pong values
+  size_t bytes;
+};
+
+SortLayout sort_layout(uint32_t n, bool kv) {
+  SortLayout L;
+  const Geometry g4 = make_geometry(n, 4, kv), g7 = make_geometry(n, 7, kv);
+  L.ms_bytes = g4.bytes > g7.bytes ? g4.bytes : g7.bytes;
+  L.off_keys = align_up(L.ms_bytes, 256);
+  L.off_vals = align_up(L.off_keys + size_t(n) * 4, 256);
+  L.bytes = kv ? align_up(L.off_vals + size_t(n) * 4, 256) : L.off_vals;
+  return L;
+}
+
+gms_status sort_impl(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                     bool kv, void* scratch, size_t scratch_bytes, cudaStream_t stream) {
+  if (n == 0) return GMS_SUCCESS;
+  if (kin == nullptr || kout == nullptr || scratch == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (kv && (vin == nullptr || vout == nullptr)) return GMS_ERROR_INVALID_VALUE;
+  const SortLayout L = sort_layout(n, kv);
+  if (scratch_bytes < L.bytes) return GMS_ERROR_SCRATCH_TOO_SMALL;
+  auto* base = static_cast<unsigned char*>(scratch);
+  uint32_t* tk = reinterpret_cast<uint32_t*>(base + L.off_keys);
+  uint32_t* tv = kv ? reinterpret_cast<uint32_t*>(base + L.off_vals) : nullptr;
+
+  // Digit schedule and buffer ping-pong of src/api/multisplit_sort.cuh:333-363.
+  struct Pass {
+    uint32_t shift, buckets;
+    const uint32_t *ki, *vi;
+    uint32_t *ko, *vo;
+  };
+  const Pass passes[5] = {{0, 16, kin, vin, kout, vout},
+                          {4, 128, kout, vout, tk, tv},
+                          {11, 128, tk, tv, kout, vout},
+                          {18, 128, kout, vout, tk, tv},
+                          {25, 128, tk, tv, kout, vout}};
+  for (const Pass& p : passes) {
+    gms_bucket_desc d{};
+    d.kind = GMS_BUCKET_BITS;
+    d.num_buckets = p.buckets;
+    d.shift = p.shift;
+    gms_status st =
+        multisplit_impl(p.ki, kv ? p.vi : nullptr, p.ko, kv ? p.vo : nullptr, n, &d, kv, scratch, L.ms_bytes,
+                        STAGE_ALL, stream);
+    if (st != GMS_SUCCESS) return st;
+  }
+  return GMS_SUCCESS;
+}
+
+gms_status compaction_impl(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n,
+                           const gms_bucket_desc* desc, bool kv, void* scratch, size_t scratch_bytes,
+                           uint32_t* h_num0, cudaStream_t stream) {
+  if (desc == nullptr || desc->num_buckets != 2) return GMS_ERROR_INVALID_VALUE;
+  gms_status st = multisplit_impl(kin, vin, kout, vout, n, desc, kv, scratch, scratch_bytes, STAGE_ALL, stream);
+  if (st != GMS_SUCCESS || h_num0 == nullptr) return st;
+  if (n == 0) {
+    *h_num0 = 0;
+    return GMS_SUCCESS;
+  }
+  // Start of bucket 1 = number of bucket-0 keys (multisplit2_compaction.cuh:541-542).
+  const Geometry g = make_geometry(n, 1, kv);
+  const auto* matrix = static_cast<const unsigned char*>(scratch) + g.off_matrix;
+  cudaError_t e = cudaMemcpyAsync(h_num0, matrix + size_t(g.num_tiles) * 4, sizeof(uint32_t),
+                                  cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  return cuda_status(e);
+}
+
+}  // namespace
+
+uint32_t tile_keys(int logb, bool kv) {
+#define GMS_TILE_CASE(L) \
+  case L: return kv ? tile_of<L, true>() : tile_of<L, false>();
+  switch (logb) {
+    GMS_TILE_CASE(1)
+    GMS_TILE_CASE(2)
+    GMS_TILE_CASE(3)
+    GMS_TILE_CASE(4)
+    GMS_TILE_CASE(5)
+    GMS_TILE_CASE(6)
+    GMS_TILE_CASE(7)
+    GMS_TILE_CASE(8)
+    default: return 0;
+  }
+#undef GMS_TILE_CASE
+}
+
+cudaError_t run_scan(uint32_t* data, uint32_t m, uint64_t* status, ScratchHeader* hdr, cudaStream_t stream) {
+  if (m == 0) return cudaSuccess;
+  const uint32_t chunks = (m + SCAN_CHUNK - 1) / SCAN_CHUNK;
+  scan_kernel<<<chunks, SCAN_THREADS, 0, stream>>>(data, m, status, hdr);
+  return cudaGetLastError();
+}
+
+int device_sm_count() {
+  static std::atomic<int> cached[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 132;
+  int v = cached[dev & 63].load(std::memory_order_relaxed);
+  if (v > 0) return v;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 132;
+  cached[dev & 63].store(v, std::memory_order_relaxed);
+  return v;
+}
+
+}  // namespace gms
+
+using namespace gms;
+
+extern "C" {
+
+int gms_version(void) { return 100; }
+
+const char* gms_status_string(gms_status s) {
+  switch (s) {
+    case GMS_SUCCESS: return "success";
+    case GMS_ERROR_INVALID_VALUE: return "invalid value";
+    case GMS_ERROR_UNSUPPORTED_BUCKETS: return "number of buckets must be a power of two in [2, 256]";
+    case GMS_ERROR_SCRATCH_TOO_SMALL: return "scratch buffer too small";
+    case GMS_ERROR_CUDA: return "CUDA runtime error";
+    case GMS_ERROR_DEVICE_TIMEOUT: return "device-side wait timed out";
+    case GMS_ERROR_NOT_SUPPORTED: return "not supported";
+  }
+  return "unknown status";
+}
+
+int gms_last_cuda_error(void) { return g_last_cuda_error; }
+
+gms_status gms_read_device_error(const void* d_scratch, uint32_t* h_code, gms_stream_t stream) {
+  if (d_scratch == nullptr || h_code == nullptr) return GMS_ERROR_INVALID_VALUE;
+  cudaError_t e = cudaMemcpyAsync(h_code, d_scratch, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  return *h_code == 0 ? GMS_SUCCESS : GMS_ERROR_DEVICE_TIMEOUT;
+}
+
+gms_status gms_multisplit_scratch_bytes(uint32_t max_elements, uint32_t num_buckets, int key_value,
+                                        size_t* bytes) {
+  int logb = 0;
+  if (bytes == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (!valid_buckets(num_buckets, &logb)) return GMS_ERROR_UNSUPPORTED_BUCKETS;
+  *bytes = make_geometry(max_elements, logb, key_value != 0).bytes;
+  return GMS_SUCCESS;
+}
+
+gms_status gms_multisplit_geometry(uint32_t n, uint32_t num_buckets, int key_value, uint32_t* tile_keys_out,
+                                   uint32_t* num_tiles, size_t* matrix_offset_bytes) {
+  int logb = 0;
+  if (!valid_buckets(num_buckets, &logb)) return GMS_ERROR_UNSUPPORTED_BUCKETS;
+  const Geometry g = make_geometry(n, logb, key_value != 0);
+  if (tile_keys_out) *tile_keys_out = g.tile;
+  if (num_tiles) *num_tiles = g.num_tiles;
+  if (matrix_offset_bytes) *matrix_offset_bytes = g.off_matrix;
+  return GMS_SUCCESS;
+}
+
+gms_status gms_multisplit_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n,
+                                   const gms_bucket_desc* desc, void* d_scratch, size_t scratch_bytes,
+                                   uint32_t* h_offsets, gms_stream_t stream) {
+  gms_status st = multisplit_impl(d_key_in, nullptr, d_key_out, nullptr, n, desc, false, d_scratch, scratch_bytes,
+                                  STAGE_ALL, stream);
+  if (st != GMS_SUCCESS || h_offsets == nullptr) return st;
+  int logb = 0;
+  valid_buckets(desc->num_buckets, &logb);
+  return copy_offsets(d_scratch, n, logb, false, h_offsets, stream);
+}
+
+gms_status gms_multisplit_key_value(const uint32_t* d_key_in, const uint32_t* d_value_in, uint32_t* d_key_out,
+                                    uint32_t* d_value_out, uint32_t n, const gms_bucket_desc* desc,
+                                    void* d_scratch, size_t scratch_bytes, uint32_t* h_offsets,
+                                    gms_stream_t stream) {
+  gms_status st = multisplit_impl(d_key_in, d_value_in, d_key_out, d_value_out, n, desc, true, d_scratch,
+                                  scratch_bytes, STAGE_ALL, stream);
+  if (st != GMS_SUCCESS || h_offsets == nullptr) return st;
+  int logb = 0;
+  valid_buckets(desc->num_buckets, &logb);
+  return copy_offsets(d_scratch, n, logb, true, h_offsets, stream);
+}
+
+gms_status gms_multisplit_prescan(const uint32_t* d_key_in, uint32_t n, const gms_bucket_desc* desc, int key_value,
+                                  void* d_scratch, size_t scratch_bytes, gms_stream_t stream) {
+  return multisplit_impl(d_key_in, nullptr, nullptr, nullptr, n, desc, key_value != 0, d_scratch, scratch_bytes,
+                         STAGE_PRESCAN, stream);
+}
+
+gms_status gms_multisplit_scan(uint32_t n, const gms_bucket_desc* desc, int key_value, void* d_scratch,
+                               size_t scratch_bytes, gms_stream_t stream) {
+  return multisplit_impl(nullptr, nullptr, nullptr, nullptr, n, desc, key_value != 0, d_scratch, scratch_bytes,
+                         STAGE_SCAN, stream);
+}
+
+gms_status gms_multisplit_postscan(const uint32_t* d_key_in, const uint32_t* d_value_in, uint32_t* d_key_out,
+                                   uint32_t* d_value_out, uint32_t n, const gms_bucket_desc* desc,
+                                   void* d_scratch, size_t scratch_bytes, gms_stream_t stream) {
+  return multisplit_impl(d_key_in, d_value_in, d_key_out, d_value_out, n, desc, d_value_in != nullptr, d_scratch,
+                         scratch_bytes, STAGE_POSTSCAN, stream);
+}
+
+gms_status gms_sort_7bit_scratch_bytes(uint32_t max_elements, int key_value, size_t* bytes) {
+  if (bytes == nullptr) return GMS_ERROR_INVALID_VALUE;
+  *bytes = sort_layout(max_elements, key_value != 0).bytes;
+  return GMS_SUCCESS;
+}
+
+gms_status gms_sort_7bit_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n, void* d_scratch,
+                                  size_t scratch_bytes, gms_stream_t stream) {
+  return sort_impl(d_key_in, d_key_out, nullptr, nullptr, n, false, d_scratch, scratch_bytes, stream);
+}
+
+gms_status gms_sort_7bit_key_value(const uint32_t* d_key_in, uint32_t* d_key_out, const uint32_t* d_value_in,
+                                   uint32_t* d_value_out, uint32_t n, void* d_scratch, size_t scratch_bytes,
+                                   gms_stream_t stream) {
+  return sort_impl(d_key_in, d_key_out, d_value_in, d_value_out, n, true, d_scratch, scratch_bytes, stream);
+}
+
+gms_status gms_compaction_scratch_bytes(uint32_t max_elements, int key_value, size_t* bytes) {
+  return gms_multisplit_scratch_bytes(max_elements, 2, key_value, bytes);
+}
+
+gms_status gms_compaction_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n,
+                                   const gms_bucket_desc* desc, void* d_scratch, size_t scratch_bytes,
+                                   uint32_t* h_num_bucket0, gms_stream_t stream) {
+  return compaction_impl(d_key_in, nullptr, d_key_out, nullptr, n, desc, false, d_scratch, scratch_bytes,
+                         h_num_bucket0, stream);
+}
+
+gms_status gms_compaction_key_value(const uint32_t* d_key_in, const uint32_t* d_value_in, uint32_t* d_key_out,
+                                    uint32_t* d_value_out, uint32_t n, const gms_bucket_desc* desc,
+                                    void* d_scratch, size_t scratch_bytes, uint32_t* h_num_bucket0,
+                                    gms_stream_t stream) {
+  return compaction_impl(d_key_in, d_value_in, d_key_out, d_value_out, n, desc, true, d_scratch, scratch_bytes,
+                         h_num_bucket0, stream);
+}
+
+gms_status gms_histogram(const uint32_t* d_key_in, uint32_t n, const gms_bucket_desc* desc, int32_t* d_hist,
+                         gms_stream_t stream) {
+  int logb = 0;
+  gms_status st = check_desc(desc, &logb);
+  if (st != GMS_SUCCESS) return st;
+  if (d_hist == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (n == 0) return GMS_SUCCESS;
+  if (d_key_in == nullptr) return GMS_ERROR_INVALID_VALUE;
+  return cuda_status(dispatch_hist(desc->kind, d_key_in, n, logb, to_params(desc), d_hist, stream));
+}
+
+gms_status gms_histogram_even(const uint32_t* d_key_in, uint32_t n, int32_t* d_hist, uint32_t num_bins,
+                              uint32_t lower, uint32_t upper, float inverse_delta, gms_stream_t stream) {
+  (void)upper;  // the reference kernels take it but bin with lower and inverse_delta only
+  gms_bucket_desc d{};
+  d.kind = GMS_BUCKET_EVEN_FLOAT;
+  d.num_buckets = num_bins;
+  d.lower = lower;
+  d.inverse_delta = inverse_delta;
+  return gms_histogram(d_key_in, n, &d, d_hist, stream);
+}
+
+gms_status gms_histogram_range(const uint32_t* d_key_in, uint32_t n, int32_t* d_hist, uint32_t num_bins,
+                               const uint32_t* d_levels, gms_stream_t stream) {
+  gms_bucket_desc d{};
+  d.kind = GMS_BUCKET_RANGE;
+  d.num_buckets = num_bins;
+  d.d_splitters = d_levels;
+  return gms_histogram(d_key_in, n, &d, d_hist, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,189 @@
+// Device-side building blocks shared by every kernel of the library:
+// PTX wrappers (mbarrier, bulk async copy, relaxed global accesses), bounded
+// waits that record an error instead of hanging, the scratch header, and the
+// bucket identifiers.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gms {
+
+// ----------------------------------------------------------------- errors
+enum DeviceError : uint32_t {
+  DEV_OK = 0,
+  DEV_ERR_BULK_COPY_TIMEOUT = 1,  // a bulk copy into shared memory did not complete in time
+  DEV_ERR_LOOKBACK_TIMEOUT = 2,   // a scan look-back waited too long for a predecessor
+  DEV_ERR_BAD_OFFSET = 3,         // a computed position fell outside the tile or the output (not written)
+};
+
+// First 256 bytes of every scratch buffer.
+struct ScratchHeader {
+  uint32_t error;       // first DeviceError recorded in the current call
+  uint32_t error_info;  // block that recorded it
+  uint32_t ticket;      // scan chunk ticket counter
+  uint32_t reserved[61];
+};
+static_assert(sizeof(ScratchHeader) == 256, "header is 256 bytes");
+
+// Wall-clock bound for every spin in the library (nanoseconds).
+constexpr uint64_t kWaitLimitNs = 1000000000ull;  // 1 s
+
+__device__ __forceinline__ uint64_t global_timer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void record_error(ScratchHeader* h, uint32_t code) {
+  if (atomicCAS(&h->error, 0u, code) == 0u) h->error_info = blockIdx.x;
+}
+
+// True once any block of the current call has recorded an error; later blocks
+// then skip their waits so a failing call ends quickly.
+__device__ __forceinline__ bool error_recorded(const ScratchHeader* h) {
+  return *reinterpret_cast<const volatile uint32_t*>(&h->error) != 0u;
+}
+
+// ------------------------------------------------------------ PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Make an initialised mbarrier visible to the async (bulk copy) proxy.
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Wait for phase `parity` of an mbarrier, giving up after kWaitLimitNs.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_timer_ns();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_timer_ns() - t0 > kWaitLimitNs) return false;
+  }
+}
+
+// One-dimensional bulk copy global -> shared (the TMA engine's non-tensor path).
+// dst and src 16-byte aligned, bytes a multiple of 16; completion is signalled
+// on `bar` as transaction bytes.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void st_relaxed_u64(uint64_t* p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ uint4 ld_nc_v4(const uint32_t* p) {
+  uint4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// ----------------------------------------------------- bucket identifiers
+// Kinds mirror gms_bucket_kind in include/gpumultisplit.h.
+enum BucketKind : int {
+  KIND_DELTA = 0,
+  KIND_DIV = 1,
+  KIND_BITS = 2,
+  KIND_RANGE = 3,
+  KIND_MASK = 4,
+  KIND_EVEN_FLOAT = 5,
+  NUM_KINDS = 6
+};
+
+struct BucketParams {
+  uint32_t shift;
+  uint32_t param;
+  uint32_t lower;
+  float inverse_delta;
+  const uint32_t* splitters;  // RANGE only (device memory, B entries)
+};
+
+// A bucket identifier for B = 2^LOGB buckets.  `s_split` is a shared-memory
+// copy of the splitters (RANGE only), filled by load_splitters().
+template <int KIND, int LOGB>
+struct Identifier {
+  static constexpr uint32_t B = 1u << LOGB;
+  BucketParams p;
+  const uint32_t* s_split;
+
+  __device__ __forceinline__ uint32_t operator()(uint32_t key) const {
+    if constexpr (KIND == KIND_DELTA) {
+      // key * B >> 32 with B = 2^LOGB is the top LOGB bits of the key.
+      return key >> (32 - LOGB);
+    } else if constexpr (KIND == KIND_DIV) {
+      return (key / p.param) & (B - 1);
+    } else if constexpr (KIND == KIND_BITS) {
+      return (key >> p.shift) & (B - 1);
+    } else if constexpr (KIND == KIND_RANGE) {
+      // Largest i with s[i] <= key (= upper_bound - 1); -1 (wrapped to B-1)
+      // when key < s[0].  Branch-free binary search over B sorted splitters.
+      uint32_t pos = 0;
+#pragma unroll
+      for (uint32_t step = B >> 1; step >= 1; step >>= 1) {
+        pos += (s_split[pos + step] <= key) ? step : 0u;
+      }
+      return (key < s_split[0]) ? (B - 1) : pos;
+    } else if constexpr (KIND == KIND_MASK) {
+      return (key & p.param) ? 1u : 0u;
+    } else {  // KIND_EVEN_FLOAT
+      const float x = __fmul_rn(__uint2float_rn(key - p.lower), p.inverse_delta);
+      return __float2uint_rz(x) & (B - 1);
+    }
+  }
+};
+
+// Copy the RANGE splitters into shared memory (no-op for other kinds).
+template <int KIND, int LOGB>
+__device__ __forceinline__ void load_splitters(uint32_t* s_split, const BucketParams& p) {
+  if constexpr (KIND == KIND_RANGE) {
+    for (uint32_t i = threadIdx.x; i < (1u << LOGB); i += blockDim.x) s_split[i] = p.splitters[i];
+  }
+}
+
+}  // namespace gms

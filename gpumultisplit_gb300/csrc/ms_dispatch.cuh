@@ -1,0 +1,114 @@
+// Launchers for one identifier kind: picks the compiled tile instance for
+// log2 B and key/value, sets its shared-memory limit once per device, and
+// launches prescan -> scan -> postscan on the caller's stream.
+// Included by exactly one inst_*.cu per kind (explicit instantiation).
+#pragma once
+
+#include <atomic>
+
+#include "histogram_kernels.cuh"
+#include "ms_host.h"
+#include "multisplit_kernels.cuh"
+
+namespace gms {
+
+// Raise a kernel's dynamic shared-memory limit once per device (bit per device id).
+template <class Kernel>
+inline cudaError_t ensure_smem_limit(Kernel k, size_t bytes, std::atomic<uint64_t>& done_mask) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = 1ull << (dev & 63);
+  if (done_mask.load(std::memory_order_acquire) & bit) return cudaSuccess;
+  e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+  if (e == cudaSuccess) done_mask.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
+
+template <int KIND, int LOGB, bool KV>
+cudaError_t run_multisplit_t(const MsCall& c, int stages) {
+  using S = TileShape<LOGB, KV>;
+  using C = TileCfg<LOGB, S::WARPS, S::IPT, KV>;
+  const Geometry g = make_geometry(c.n, LOGB, KV);
+  if (g.num_tiles == 0) return cudaSuccess;
+  auto* hdr = reinterpret_cast<ScratchHeader*>(c.scratch);
+  auto* status = reinterpret_cast<uint64_t*>(c.scratch + g.off_status);
+  auto* matrix = reinterpret_cast<uint32_t*>(c.scratch + g.off_matrix);
+
+  if (stages & STAGE_PRESCAN) {
+    prescan_kernel<C, KIND><<<g.num_tiles, C::THREADS, 0, c.stream>>>(c.kin, c.n, g.num_tiles, matrix, c.bp, hdr,
+                                                                      status, g.num_chunks);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (stages & STAGE_SCAN) {
+    cudaError_t e = run_scan(matrix, g.m, status, hdr, c.stream);
+    if (e != cudaSuccess) return e;
+  }
+  if (stages & STAGE_POSTSCAN) {
+    static std::atomic<uint64_t> smem_done{0};
+    auto kern = postscan_kernel<C, KIND>;
+    cudaError_t e = ensure_smem_limit(kern, C::POST_SMEM, smem_done);
+    if (e != cudaSuccess) return e;
+    kern<<<g.num_tiles, C::THREADS, C::POST_SMEM, c.stream>>>(c.kin, c.vin, c.kout, c.vout, c.n, g.num_tiles, matrix,
+                                                             c.bp, hdr);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+template <int KIND, bool KV>
+cudaError_t run_multisplit_kv(const MsCall& c, int stages) {
+  switch (c.logb) {
+    case 1: return run_multisplit_t<KIND, 1, KV>(c, stages);
+    case 2: return run_multisplit_t<KIND, 2, KV>(c, stages);
+    case 3: return run_multisplit_t<KIND, 3, KV>(c, stages);
+    case 4: return run_multisplit_t<KIND, 4, KV>(c, stages);
+    case 5: return run_multisplit_t<KIND, 5, KV>(c, stages);
+    case 6: return run_multisplit_t<KIND, 6, KV>(c, stages);
+    case 7: return run_multisplit_t<KIND, 7, KV>(c, stages);
+    case 8: return run_multisplit_t<KIND, 8, KV>(c, stages);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int KIND>
+cudaError_t run_multisplit(const MsCall& c, int stages) {
+  return c.kv ? run_multisplit_kv<KIND, true>(c, stages) : run_multisplit_kv<KIND, false>(c, stages);
+}
+
+template <int KIND, int LOGB>
+cudaError_t run_histogram_t(const uint32_t* keys, uint32_t n, const BucketParams& bp, int32_t* hist,
+                            cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  const uint32_t chunks = (n + HIST_CHUNK - 1) / HIST_CHUNK;
+  const uint32_t cap = uint32_t(device_sm_count()) * 8u;
+  const uint32_t grid = chunks < cap ? chunks : cap;
+  histogram_kernel<LOGB, KIND><<<grid, HIST_THREADS, 0, stream>>>(keys, n, hist, bp);
+  return cudaGetLastError();
+}
+
+template <int KIND>
+cudaError_t run_histogram(const uint32_t* keys, uint32_t n, int logb, const BucketParams& bp, int32_t* hist,
+                          cudaStream_t stream) {
+  switch (logb) {
+    case 1: return run_histogram_t<KIND, 1>(keys, n, bp, hist, stream);
+    case 2: return run_histogram_t<KIND, 2>(keys, n, bp, hist, stream);
+    case 3: return run_histogram_t<KIND, 3>(keys, n, bp, hist, stream);
+    case 4: return run_histogram_t<KIND, 4>(keys, n, bp, hist, stream);
+    case 5: return run_histogram_t<KIND, 5>(keys, n, bp, hist, stream);
+    case 6: return run_histogram_t<KIND, 6>(keys, n, bp, hist, stream);
+    case 7: return run_histogram_t<KIND, 7>(keys, n, bp, hist, stream);
+    case 8: return run_histogram_t<KIND, 8>(keys, n, bp, hist, stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace gms
+
+#define GMS_INSTANTIATE_KIND(K)                                                                        \
+  template cudaError_t gms::run_multisplit<K>(const gms::MsCall&, int);                                \
+  template cudaError_t gms::run_histogram<K>(const uint32_t*, uint32_t, int, const gms::BucketParams&, \
+                                             int32_t*, cudaStream_t);

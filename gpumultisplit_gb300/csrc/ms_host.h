@@ -1,0 +1,81 @@
+// Host-side internals shared by the C ABI (capi.cu) and the per-identifier
+// instantiation units (inst_*.cu): tile geometry, scratch layout, launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "gms_device.cuh"
+
+namespace gms {
+
+// Tile shape per (log2 B, key/value).  Keys per tile = WARPS * 32 * IPT.
+// 4096-key tiles: at B = 256 the count matrix is 1 byte per key.
+template <int LOGB, bool KV>
+struct TileShape {
+  static constexpr int WARPS = 8;
+  static constexpr int IPT = 16;
+};
+
+uint32_t tile_keys(int logb, bool kv);
+
+constexpr uint32_t kScanChunk = 4096;  // SCAN_CHUNK in scan_kernels.cuh
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Scratch layout of one multisplit: [header 256 B][count matrix u32 x B*tiles][scan status u64 x chunks].
+// The matrix always starts at byte 256, whatever n is.
+struct Geometry {
+  uint32_t tile = 0;
+  uint32_t num_tiles = 0;
+  uint32_t m = 0;           // B * num_tiles
+  uint32_t num_chunks = 0;  // scan chunks
+  size_t off_status = 0;
+  size_t off_matrix = 0;
+  size_t bytes = 0;
+};
+
+inline Geometry make_geometry(uint32_t n, int logb, bool kv) {
+  Geometry g;
+  g.tile = tile_keys(logb, kv);
+  g.num_tiles = uint32_t((uint64_t(n) + g.tile - 1) / g.tile);
+  g.m = (1u << logb) * g.num_tiles;
+  g.num_chunks = (g.m + kScanChunk - 1) / kScanChunk;
+  g.off_matrix = sizeof(ScratchHeader);
+  g.off_status = align_up(g.off_matrix + size_t(g.m) * 4, 256);
+  g.bytes = align_up(g.off_status + size_t(g.num_chunks) * 8, 256);
+  return g;
+}
+
+enum Stage : int { STAGE_PRESCAN = 1, STAGE_SCAN = 2, STAGE_POSTSCAN = 4, STAGE_ALL = 7 };
+
+struct MsCall {
+  const uint32_t* kin = nullptr;
+  const uint32_t* vin = nullptr;
+  uint32_t* kout = nullptr;
+  uint32_t* vout = nullptr;
+  uint32_t n = 0;
+  int logb = 1;
+  bool kv = false;
+  BucketParams bp{};
+  unsigned char* scratch = nullptr;  // laid out as make_geometry(n, logb, kv)
+  cudaStream_t stream = nullptr;
+};
+
+// Runs the requested stages (a mask of Stage) of one multisplit.  Defined per
+// identifier kind in inst_*.cu.
+template <int KIND>
+cudaError_t run_multisplit(const MsCall& c, int stages);
+
+// Histogram of keys[0..n) into hist[0..2^logb), accumulated with atomics.
+template <int KIND>
+cudaError_t run_histogram(const uint32_t* keys, uint32_t n, int logb, const BucketParams& bp, int32_t* hist,
+                          cudaStream_t stream);
+
+cudaError_t run_scan(uint32_t* data, uint32_t m, uint64_t* status, ScratchHeader* hdr, cudaStream_t stream);
+
+int device_sm_count();
+
+}  // namespace gms

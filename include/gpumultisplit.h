@@ -1,0 +1,186 @@
+/*
+ * gpumultisplit.h -- C ABI of the GB300 (sm_103a) multisplit library.
+ *
+ * Plain pointers and sizes only: every pointer named d_* is a device pointer,
+ * every h_* pointer is host memory.  All calls are asynchronous on `stream`
+ * unless they say otherwise; a null stream is the legacy default stream, the
+ * stream every reference entry point runs on.
+ *
+ * Each entry point cites the reference interface it replaces (paths inside the
+ * owensgroup/GpuMultisplit tree).  The reference instantiates its kernels on a
+ * user functor type; a precompiled ABI cannot, so the bucket identifier is a
+ * POD descriptor (gms_bucket_desc) that covers the functors the reference and
+ * its drivers use.  The drop-in C++ headers in include/gpumultisplit/ map
+ * functor types onto descriptors.
+ *
+ * Scratch: the reference's contexts cudaMalloc a bucket-count matrix plus CUB
+ * scan storage (src/api/multisplit.cuh:50-74).  Here the caller owns one
+ * scratch buffer whose size *_scratch_bytes() reports; the library never
+ * allocates.  A scratch buffer serves one call at a time (calls that overlap
+ * on the GPU and share a buffer race).
+ */
+#ifndef GPUMULTISPLIT_H_
+#define GPUMULTISPLIT_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same object as cudaStream_t; declared here so the header needs no CUDA headers. */
+typedef struct CUstream_st* gms_stream_t;
+
+typedef enum gms_status {
+  GMS_SUCCESS = 0,
+  GMS_ERROR_INVALID_VALUE = 1,       /* null pointer, bad kind, n over capacity ... */
+  GMS_ERROR_UNSUPPORTED_BUCKETS = 2, /* num_buckets not a power of two in [2, 256] */
+  GMS_ERROR_SCRATCH_TOO_SMALL = 3,
+  GMS_ERROR_CUDA = 4,                /* a CUDA runtime call failed; see gms_last_cuda_error() */
+  GMS_ERROR_DEVICE_TIMEOUT = 5,      /* a bounded device-side wait gave up (read by gms_read_device_error) */
+  GMS_ERROR_NOT_SUPPORTED = 6
+} gms_status;
+
+/*
+ * Bucket identifier kinds.  Every kind yields a value that is reduced modulo
+ * num_buckets (the reference's GPU kernels decode a bucket id from its low
+ * log2(B) bits with ballots, src/kernels/bms/bms_prescan.cuh:480-517, so an
+ * out-of-range id wraps the same way there).
+ *
+ *  GMS_BUCKET_DELTA       key * B >> 32 (64-bit product): B equal-width key ranges.
+ *  GMS_BUCKET_DIV         key / param   (delta_func, README.md:85-91, src/main/main_multisplit.cu:41-47).
+ *  GMS_BUCKET_BITS        (key >> shift) & (B-1)  (ms_bucket_sort_*bit<shift>, src/api/multisplit_sort.cuh:63-98;
+ *                          compaction's test_bucket<1> = key & 1, src/main/main_compaction.cu:26-31).
+ *  GMS_BUCKET_RANGE       upper_bound(d_splitters[0..B), key) - 1 (cub::UpperBound on the level array,
+ *                          src/kernels/histogram/multisplit2_histograms.cuh:434); keys below
+ *                          d_splitters[0] give -1, i.e. bucket B-1 after the wrap.
+ *  GMS_BUCKET_MASK        (key & param) != 0 (a two-bucket predicate).
+ *  GMS_BUCKET_EVEN_FLOAT  (uint32)((float)(key - lower) * inverse_delta), float round-to-nearest
+ *                          convert and multiply, truncating saturating convert back
+ *                          (src/kernels/histogram/multisplit2_histograms.cuh:60).
+ */
+typedef enum gms_bucket_kind {
+  GMS_BUCKET_DELTA = 0,
+  GMS_BUCKET_DIV = 1,
+  GMS_BUCKET_BITS = 2,
+  GMS_BUCKET_RANGE = 3,
+  GMS_BUCKET_MASK = 4,
+  GMS_BUCKET_EVEN_FLOAT = 5
+} gms_bucket_kind;
+
+typedef struct gms_bucket_desc {
+  int32_t kind;                /* gms_bucket_kind */
+  uint32_t num_buckets;        /* B: power of two, 2..256 */
+  uint32_t shift;              /* BITS */
+  uint32_t param;              /* DIV: divisor (non-zero); MASK: mask */
+  uint32_t lower;              /* EVEN_FLOAT: lower level */
+  float inverse_delta;         /* EVEN_FLOAT: 1 / bin width */
+  const uint32_t* d_splitters; /* RANGE: B sorted splitters, device memory */
+} gms_bucket_desc;
+
+/* ---------------------------------------------------------------- info */
+int gms_version(void);
+const char* gms_status_string(gms_status s);
+/* Last CUDA error code seen by a call that returned GMS_ERROR_CUDA (per thread). */
+int gms_last_cuda_error(void);
+
+/* Device-side error word of a scratch buffer: 0 if the last call that used it
+ * finished every bounded wait, else a non-zero code.  Synchronises `stream`. */
+gms_status gms_read_device_error(const void* d_scratch, uint32_t* h_code, gms_stream_t stream);
+
+/* ------------------------------------------------------------ multisplit */
+/* Replaces multisplit_allocate_key_only / _key_value (src/api/multisplit.cuh:50-74):
+ * scratch bytes for calls with n <= max_elements. */
+gms_status gms_multisplit_scratch_bytes(uint32_t max_elements, uint32_t num_buckets, int key_value,
+                                        size_t* bytes);
+
+/* Replaces multisplit_key_only (src/api/multisplit.cuh:81-197).  Stable: buckets
+ * ascending, input order kept inside a bucket.  If h_offsets is non-null the
+ * call synchronises and writes the B bucket start offsets there (:143-149). */
+gms_status gms_multisplit_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n,
+                                   const gms_bucket_desc* desc, void* d_scratch, size_t scratch_bytes,
+                                   uint32_t* h_offsets, gms_stream_t stream);
+
+/* Replaces multisplit_key_value (src/api/multisplit.cuh:199-313); values move with their keys. */
+gms_status gms_multisplit_key_value(const uint32_t* d_key_in, const uint32_t* d_value_in,
+                                    uint32_t* d_key_out, uint32_t* d_value_out, uint32_t n,
+                                    const gms_bucket_desc* desc, void* d_scratch, size_t scratch_bytes,
+                                    uint32_t* h_offsets, gms_stream_t stream);
+
+/* The three stages of one multisplit, callable one by one (the reference runs
+ * them as prescan kernel, cub::DeviceScan::ExclusiveSum, postscan kernel:
+ * src/api/multisplit.cuh:212-272).  Scratch sized by gms_multisplit_scratch_bytes
+ * for the same n, B and key_value.  After gms_multisplit_scan the count matrix in
+ * scratch holds global offsets, bucket-major: offset(b, tile) at b*num_tiles+tile. */
+gms_status gms_multisplit_prescan(const uint32_t* d_key_in, uint32_t n, const gms_bucket_desc* desc,
+                                  int key_value, void* d_scratch, size_t scratch_bytes, gms_stream_t stream);
+gms_status gms_multisplit_scan(uint32_t n, const gms_bucket_desc* desc, int key_value, void* d_scratch,
+                               size_t scratch_bytes, gms_stream_t stream);
+gms_status gms_multisplit_postscan(const uint32_t* d_key_in, const uint32_t* d_value_in, uint32_t* d_key_out,
+                                   uint32_t* d_value_out, uint32_t n, const gms_bucket_desc* desc,
+                                   void* d_scratch, size_t scratch_bytes, gms_stream_t stream);
+
+/* Tile geometry the library uses for (n, B, key_value): keys per tile and number
+ * of tiles (the reference's size_sub_prob / num_sub_prob, src/api/multisplit.cuh:29-47),
+ * and the byte offset of the count matrix inside scratch. */
+gms_status gms_multisplit_geometry(uint32_t n, uint32_t num_buckets, int key_value, uint32_t* tile_keys,
+                                   uint32_t* num_tiles, size_t* matrix_offset_bytes);
+
+/* ----------------------------------------------------------------- sort */
+/* Replaces multisplit_sort_7bit_allocate / _allocate_pairs (src/api/multisplit_sort.cuh:151-191).
+ * Includes the ping-pong key (and value) buffer the reference keeps in d_key_temp_ms. */
+gms_status gms_sort_7bit_scratch_bytes(uint32_t max_elements, int key_value, size_t* bytes);
+
+/* Replaces multisplit_sort_7bit (src/api/multisplit_sort.cuh:320-364): LSD radix
+ * sort, digits [0,4) then [4,11) [11,18) [18,25) [25,32).  d_key_in is not modified. */
+gms_status gms_sort_7bit_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n, void* d_scratch,
+                                  size_t scratch_bytes, gms_stream_t stream);
+
+/* Replaces multisplit_sort_7bit_pairs (src/api/multisplit_sort_pairs.cuh:21-65).
+ * Argument order follows the reference: (key_in, key_out, value_in, value_out). */
+gms_status gms_sort_7bit_key_value(const uint32_t* d_key_in, uint32_t* d_key_out, const uint32_t* d_value_in,
+                                   uint32_t* d_value_out, uint32_t n, void* d_scratch, size_t scratch_bytes,
+                                   gms_stream_t stream);
+
+/* ----------------------------------------------------------- compaction */
+/* Replaces compaction_allocate_key_only / _key_value
+ * (src/kernels/compaction/multisplit2_compaction.cuh:491-517). */
+gms_status gms_compaction_scratch_bytes(uint32_t max_elements, int key_value, size_t* bytes);
+
+/* Replaces compaction_key_only / compaction_key_value
+ * (src/kernels/compaction/multisplit2_compaction.cuh:525-573): a stable two-bucket
+ * multisplit, bucket 0 first.  desc->num_buckets must be 2.  Like the reference
+ * it synchronises and returns the bucket-0 count in *h_num_bucket0 (:541-547). */
+gms_status gms_compaction_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n,
+                                   const gms_bucket_desc* desc, void* d_scratch, size_t scratch_bytes,
+                                   uint32_t* h_num_bucket0, gms_stream_t stream);
+gms_status gms_compaction_key_value(const uint32_t* d_key_in, const uint32_t* d_value_in, uint32_t* d_key_out,
+                                    uint32_t* d_value_out, uint32_t n, const gms_bucket_desc* desc,
+                                    void* d_scratch, size_t scratch_bytes, uint32_t* h_num_bucket0,
+                                    gms_stream_t stream);
+
+/* ------------------------------------------------------------ histogram */
+/* Adds the per-bucket counts of d_key_in[0..n) into d_hist[0..B) (the caller
+ * zeroes it first, as with the reference's atomicAdd kernels).  Generalises
+ * multisplit2_histogram_even_* / _range_* (src/kernels/histogram/multisplit2_histograms.cuh:36-699)
+ * to every identifier kind and to any n (the reference needs n to be a whole
+ * number of tiles, src/main/main_histogram.cu:76). */
+gms_status gms_histogram(const uint32_t* d_key_in, uint32_t n, const gms_bucket_desc* desc, int32_t* d_hist,
+                         gms_stream_t stream);
+
+/* multisplit2_histogram_even_* launch (src/main/main_histogram.cu:163-179) with
+ * uint32 samples: bin = (uint32)((key - lower) * inverse_delta), wrapped modulo num_bins. */
+gms_status gms_histogram_even(const uint32_t* d_key_in, uint32_t n, int32_t* d_hist, uint32_t num_bins,
+                              uint32_t lower, uint32_t upper, float inverse_delta, gms_stream_t stream);
+
+/* multisplit2_histogram_range_* launch (src/main/main_histogram.cu:272-279):
+ * bin = upper_bound(d_levels[0..num_bins), key) - 1, wrapped modulo num_bins. */
+gms_status gms_histogram_range(const uint32_t* d_key_in, uint32_t n, int32_t* d_hist, uint32_t num_bins,
+                               const uint32_t* d_levels, gms_stream_t stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* GPUMULTISPLIT_H_ */

@@ -1,0 +1,233 @@
+/*
+ * CPU oracle for the multisplit hot path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's CPU algorithms, used by the tests,
+ * by the smoke check and as the timed CPU baseline.  The library never calls
+ * it.  Each function cites the reference code it restates (paths inside the
+ * owensgroup/GpuMultisplit tree).  It is pinned against the reference's own
+ * CPU multisplit compiled from its sources (oracle/ref_shim.cpp) through the
+ * committed golden vectors in tests/golden/.
+ */
+#include "oracle.h"
+
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* Bucket identifier.  Every kind is reduced modulo B: the reference's GPU
+ * kernels decode the bucket from its low log2(B) bits with ballots
+ * (src/kernels/bms/bms_prescan.cuh:480-517).
+ *   DELTA       key * B >> 32                     (equal-width ranges)
+ *   DIV         key / param                       (delta_func, src/main/main_multisplit.cu:41-47)
+ *   BITS        (key >> shift)                    (ms_bucket_sort_*bit, src/api/multisplit_sort.cuh:63-98)
+ *   RANGE       upper_bound(splitters, B, key) - 1 (src/kernels/histogram/multisplit2_histograms.cuh:434)
+ *   MASK        (key & param) != 0
+ *   EVEN_FLOAT  (uint32)((float)(key - lower) * inverse_delta)
+ *                                               (src/kernels/histogram/multisplit2_histograms.cuh:60)
+ */
+uint32_t oracle_bucket(const oracle_desc* d, uint32_t key) {
+  const uint32_t mask = d->num_buckets - 1u;
+  switch (d->kind) {
+    case ORACLE_DELTA:
+      return (uint32_t)(((uint64_t)key * d->num_buckets) >> 32) & mask;
+    case ORACLE_DIV:
+      return (key / d->param) & mask;
+    case ORACLE_BITS:
+      return (d->shift >= 32u ? 0u : (key >> d->shift)) & mask;
+    case ORACLE_RANGE: {
+      /* upper_bound: first index whose splitter is > key. */
+      uint32_t lo = 0, hi = d->num_buckets;
+      while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2u;
+        if (d->splitters[mid] <= key)
+          lo = mid + 1u;
+        else
+          hi = mid;
+      }
+      return (lo - 1u) & mask;
+    }
+    case ORACLE_MASK:
+      return (key & d->param) ? 1u : 0u;
+    case ORACLE_EVEN_FLOAT: {
+      /* uint32 -> float and float * float in round-to-nearest-even (the host
+       * default and CUDA's __uint2float_rn / __fmul_rn), then a truncating
+       * conversion that saturates like the GPU's cvt.rzi.u32.f32. */
+      const float x = (float)(uint32_t)(key - d->lower) * d->inverse_delta;
+      uint32_t b;
+      if (!(x > 0.0f))
+        b = 0u; /* negative, zero or NaN */
+      else if (x >= 4294967296.0f)
+        b = 0xFFFFFFFFu;
+      else
+        b = (uint32_t)x;
+      return b & mask;
+    }
+    default:
+      return 0u;
+  }
+}
+
+/* Histogram -> exclusive scan -> stable placement: cpu_multisplit_general and
+ * cpu_multisplit_pairs_general (src/cpu_functions.h:155-288).  vin/vout may be
+ * NULL (key-only).  offsets (B entries) receives the bucket starts if non-NULL. */
+static void multisplit(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                       const oracle_desc* d, uint32_t* offsets) {
+  const uint32_t B = d->num_buckets;
+  uint32_t* bins = (uint32_t*)calloc(B, sizeof(uint32_t));
+  uint32_t* next = (uint32_t*)calloc(B, sizeof(uint32_t));
+  for (uint32_t i = 0; i < n; ++i) bins[oracle_bucket(d, kin[i])]++;
+  uint32_t run = 0;
+  for (uint32_t b = 0; b < B; ++b) {
+    next[b] = run;
+    run += bins[b];
+  }
+  if (offsets) memcpy(offsets, next, B * sizeof(uint32_t));
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t b = oracle_bucket(d, kin[i]);
+    const uint32_t dst = next[b]++;
+    kout[dst] = kin[i];
+    if (vin) vout[dst] = vin[i];
+  }
+  free(bins);
+  free(next);
+}
+
+void oracle_multisplit_keys(const uint32_t* kin, uint32_t* kout, uint32_t n, const oracle_desc* d,
+                            uint32_t* offsets) {
+  multisplit(kin, kout, NULL, NULL, n, d, offsets);
+}
+
+void oracle_multisplit_pairs(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                             const oracle_desc* d, uint32_t* offsets) {
+  multisplit(kin, kout, vin, vout, n, d, offsets);
+}
+
+/* Per-tile bucket counts, bucket-major: counts[b * num_tiles + t] -- the layout
+ * checked by cpu_prescan_test (src/cpu_functions.h:55-103) and written by the
+ * prescan kernels (src/kernels/bms/bms_prescan.cuh:114).  Keys past n are not
+ * counted. */
+void oracle_tile_counts(const uint32_t* kin, uint32_t n, const oracle_desc* d, uint32_t tile, uint32_t* counts) {
+  const uint32_t num_tiles = (uint32_t)(((uint64_t)n + tile - 1) / tile);
+  memset(counts, 0, sizeof(uint32_t) * (size_t)num_tiles * d->num_buckets);
+  for (uint32_t i = 0; i < n; ++i) counts[(size_t)oracle_bucket(d, kin[i]) * num_tiles + i / tile]++;
+}
+
+/* Adds per-bucket counts into hist (the reference's histogram kernels add into
+ * a caller-zeroed int array with atomics, multisplit2_histograms.cuh:88,389). */
+void oracle_histogram(const uint32_t* kin, uint32_t n, const oracle_desc* d, int32_t* hist) {
+  for (uint32_t i = 0; i < n; ++i) hist[oracle_bucket(d, kin[i])]++;
+}
+
+/* 7-bit multisplit radix sort: a 4-bit pass then four 7-bit passes, each a
+ * stable multisplit on a bit field (src/api/multisplit_sort.cuh:320-364,
+ * src/api/multisplit_sort_pairs.cuh:21-65).  tmp_k/tmp_v hold n entries. */
+void oracle_sort_7bit(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                      uint32_t* tmp_k, uint32_t* tmp_v) {
+  static const uint32_t shifts[5] = {0, 4, 11, 18, 25};
+  static const uint32_t buckets[5] = {16, 128, 128, 128, 128};
+  const uint32_t* src_k = kin;
+  const uint32_t* src_v = vin;
+  for (int p = 0; p < 5; ++p) {
+    /* passes 0, 2, 4 write the output buffer; 1, 3 the temporary one */
+    uint32_t* dk = (p % 2 == 0) ? kout : tmp_k;
+    uint32_t* dv = (p % 2 == 0) ? vout : tmp_v;
+    oracle_desc d;
+    memset(&d, 0, sizeof(d));
+    d.kind = ORACLE_BITS;
+    d.num_buckets = buckets[p];
+    d.shift = shifts[p];
+    multisplit(src_k, dk, vin ? src_v : NULL, vin ? dv : NULL, n, &d, NULL);
+    src_k = dk;
+    src_v = dv;
+  }
+}
+
+/* Two-bucket stable multisplit; returns the bucket-0 count
+ * (src/kernels/compaction/multisplit2_compaction.cuh:525-573). */
+uint32_t oracle_compaction(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                           const oracle_desc* d) {
+  uint32_t offsets[2];
+  multisplit(kin, kout, vin, vout, n, d, offsets);
+  return n == 0 ? 0u : offsets[1];
+}
+
+/* ---------------------------------------------------------------------
+ * Multi-threaded restatement (CPU baseline): the same stable result from P
+ * contiguous chunks -- per-chunk histograms, an exclusive scan in
+ * (bucket, chunk) order, then each chunk scatters its own keys in order.
+ */
+typedef struct {
+  const uint32_t* kin;
+  uint32_t* kout;
+  const uint32_t* vin;
+  uint32_t* vout;
+  const oracle_desc* d;
+  uint32_t begin, end;
+  uint32_t* counts; /* B entries for this chunk: counts, then write cursors */
+  int phase;
+} mt_job;
+
+static void* mt_worker(void* arg) {
+  mt_job* j = (mt_job*)arg;
+  if (j->phase == 0) {
+    memset(j->counts, 0, sizeof(uint32_t) * j->d->num_buckets);
+    for (uint32_t i = j->begin; i < j->end; ++i) j->counts[oracle_bucket(j->d, j->kin[i])]++;
+  } else {
+    for (uint32_t i = j->begin; i < j->end; ++i) {
+      const uint32_t dst = j->counts[oracle_bucket(j->d, j->kin[i])]++;
+      j->kout[dst] = j->kin[i];
+      if (j->vin) j->vout[dst] = j->vin[i];
+    }
+  }
+  return NULL;
+}
+
+void oracle_multisplit_mt(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                          const oracle_desc* d, int threads) {
+  if (threads < 1) threads = 1;
+  if ((uint32_t)threads > n / 4096u + 1u) threads = (int)(n / 4096u + 1u);
+  const uint32_t B = d->num_buckets;
+  mt_job* jobs = (mt_job*)calloc((size_t)threads, sizeof(mt_job));
+  pthread_t* tid = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
+  uint32_t* counts = (uint32_t*)calloc((size_t)threads * B, sizeof(uint32_t));
+  const uint64_t per = ((uint64_t)n + threads - 1) / threads;
+  for (int t = 0; t < threads; ++t) {
+    uint64_t b = per * t, e = b + per;
+    if (b > n) b = n;
+    if (e > n) e = n;
+    jobs[t] = (mt_job){kin, kout, vin, vout, d, (uint32_t)b, (uint32_t)e, counts + (size_t)t * B, 0};
+  }
+  for (int phase = 0; phase < 2; ++phase) {
+    if (phase == 1) {
+      uint32_t run = 0;
+      for (uint32_t b = 0; b < B; ++b)
+        for (int t = 0; t < threads; ++t) {
+          const uint32_t c = counts[(size_t)t * B + b];
+          counts[(size_t)t * B + b] = run;
+          run += c;
+        }
+    }
+    for (int t = 0; t < threads; ++t) {
+      jobs[t].phase = phase;
+      if (t == 0) continue;
+      pthread_create(&tid[t], NULL, mt_worker, &jobs[t]);
+    }
+    mt_worker(&jobs[0]);
+    for (int t = 1; t < threads; ++t) pthread_join(tid[t], NULL);
+  }
+  free(counts);
+  free(tid);
+  free(jobs);
+}
+
+/* splitmix64 keys (seed, i) -> uint32, the generator of gpumultisplit_gb300/datagen.py,
+ * so the oracle can build large inputs without Python. */
+void oracle_uniform_u32(uint32_t* out, uint64_t n, uint64_t seed) {
+  for (uint64_t i = 0; i < n; ++i) {
+    uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    out[i] = (uint32_t)(z >> 32);
+  }
+}

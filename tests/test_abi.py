@@ -1,0 +1,113 @@
+"""The C-ABI library without a GPU: it loads, exports every entry point that
+include/*.h declares, and its host-only logic (scratch sizing, tile geometry,
+argument checks that fail before any CUDA call) behaves."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+import gpumultisplit_gb300 as gms
+from gpumultisplit_gb300 import _lib
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"\b(gms_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+def test_library_exports_every_declared_symbol(gms_lib):
+    decl = declared_symbols()
+    assert len(decl) >= 20
+    for name in decl:
+        assert hasattr(gms_lib, name), name
+    # and the Python binding prototypes cover the same set
+    assert decl == set(_lib.EXPORTED)
+
+
+def test_version_and_status_strings(gms_lib):
+    assert gms_lib.gms_version() >= 100
+    for s in range(7):
+        assert gms_lib.gms_status_string(s)
+
+
+def scratch_bytes(n, B, kv):
+    out = ctypes.c_size_t()
+    st = gms_lib_().gms_multisplit_scratch_bytes(n, B, kv, ctypes.byref(out))
+    return st, out.value
+
+
+def gms_lib_():
+    return gms.load()
+
+
+@pytest.mark.parametrize("B", [2, 4, 8, 16, 32, 64, 128, 256])
+@pytest.mark.parametrize("kv", [0, 1])
+def test_scratch_and_geometry(gms_lib, B, kv):
+    for n in (0, 1, 4095, 4096, 4097, 1 << 20, 1 << 28, 0xFFFFFFFF):
+        st, nbytes = scratch_bytes(n, B, kv)
+        assert st == 0
+        tile, tiles, off = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_size_t()
+        assert gms_lib.gms_multisplit_geometry(n, B, kv, ctypes.byref(tile), ctypes.byref(tiles),
+                                               ctypes.byref(off)) == 0
+        assert tiles.value == (n + tile.value - 1) // tile.value
+        assert off.value == 256  # the count matrix always starts after the 256-byte header
+        assert nbytes >= 256 + 4 * B * tiles.value
+        assert nbytes % 256 == 0
+
+
+def test_unsupported_bucket_counts(gms_lib):
+    for B in (0, 1, 3, 12, 257, 512):
+        st, _ = scratch_bytes(100, B, 0)
+        assert st == _lib.GMS_ERROR_UNSUPPORTED_BUCKETS
+
+
+def test_argument_checks_before_cuda(gms_lib):
+    """These calls fail on their arguments, before any CUDA work."""
+    d = _lib.BucketDesc(kind=_lib.GMS_BUCKET_DELTA, num_buckets=7)
+    assert gms_lib.gms_multisplit_key_only(1 << 20, 2 << 20, 10, ctypes.byref(d), 1 << 24, 1 << 20, None,
+                                           None) == _lib.GMS_ERROR_UNSUPPORTED_BUCKETS
+    d = _lib.BucketDesc(kind=99, num_buckets=8)
+    assert gms_lib.gms_multisplit_key_only(1 << 20, 2 << 20, 10, ctypes.byref(d), 1 << 24, 1 << 20, None,
+                                           None) == _lib.GMS_ERROR_INVALID_VALUE
+    d = _lib.BucketDesc(kind=_lib.GMS_BUCKET_DIV, num_buckets=8, param=0)
+    assert gms_lib.gms_multisplit_key_only(1 << 20, 2 << 20, 10, ctypes.byref(d), 1 << 24, 1 << 20, None,
+                                           None) == _lib.GMS_ERROR_INVALID_VALUE
+    d = _lib.BucketDesc(kind=_lib.GMS_BUCKET_RANGE, num_buckets=8)
+    assert gms_lib.gms_multisplit_key_only(1 << 20, 2 << 20, 10, ctypes.byref(d), 1 << 24, 1 << 20, None,
+                                           None) == _lib.GMS_ERROR_INVALID_VALUE
+    d = _lib.BucketDesc(kind=_lib.GMS_BUCKET_DELTA, num_buckets=8)
+    # scratch too small for n
+    assert gms_lib.gms_multisplit_key_only(1 << 30, 2 << 30, 1 << 20, ctypes.byref(d), 1 << 24, 1024, None,
+                                           None) == _lib.GMS_ERROR_SCRATCH_TOO_SMALL
+    # scratch not 256-byte aligned
+    assert gms_lib.gms_multisplit_key_only(1 << 20, 2 << 20, 10, ctypes.byref(d), (1 << 24) + 4, 1 << 20, None,
+                                           None) == _lib.GMS_ERROR_INVALID_VALUE
+    # in place (input and output overlap)
+    assert gms_lib.gms_multisplit_key_only(1 << 20, (1 << 20) + 16, 10, ctypes.byref(d), 1 << 24, 1 << 20, None,
+                                           None) == _lib.GMS_ERROR_INVALID_VALUE
+    # n = 0 is a no-op that succeeds
+    assert gms_lib.gms_multisplit_key_only(None, None, 0, ctypes.byref(d), None, 0, None, None) == 0
+    # compaction needs exactly two buckets
+    assert gms_lib.gms_compaction_key_only(1 << 20, 2 << 20, 10, ctypes.byref(d), 1 << 24, 1 << 20, None,
+                                           None) == _lib.GMS_ERROR_INVALID_VALUE
+
+
+def test_sort_scratch_covers_both_digit_widths(gms_lib):
+    for n in (1, 1000, 1 << 20):
+        for kv in (0, 1):
+            sb = ctypes.c_size_t()
+            assert gms_lib.gms_sort_7bit_scratch_bytes(n, kv, ctypes.byref(sb)) == 0
+            _, m16 = scratch_bytes(n, 16, kv)
+            _, m128 = scratch_bytes(n, 128, kv)
+            assert sb.value >= max(m16, m128) + 4 * n * (1 + kv)
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(ImportError):
+        _lib.load(tmp_path / "libgpumultisplit.so")

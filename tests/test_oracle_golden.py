@@ -1,0 +1,136 @@
+"""The CPU oracle, pinned against golden vectors produced by the reference's own
+CPU multisplit (tests/golden/make_golden.py), and against that reference code
+directly where it is built (oracle/_ref, only where the reference tree exists)."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from gpumultisplit_gb300 import datagen
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.uint32).tobytes()).hexdigest()
+
+
+def gen_keys(case):
+    dist, n, seed = case["dist"], case["n"], case.get("seed", 0)
+    if dist == "explicit":
+        return np.array(case["keys_in"], np.uint32)
+    if dist == "uniform":
+        return datagen.as_u32(datagen.uniform_u32(n, seed))
+    if dist == "zipf":
+        return datagen.as_u32(datagen.zipf_u32(n, seed, distinct=1 << 12))
+    if dist == "and4":
+        return datagen.as_u32(datagen.and4_u32(n, seed))
+    if dist == "iota":
+        return np.arange(n, dtype=np.uint32)
+    raise ValueError(dist)
+
+
+def desc_of(o, case):
+    spl = None
+    if case.get("kind") == o.RANGE:
+        spl = datagen.as_u32(datagen.range_splitters(case["buckets"], case["splitter_seed"]))
+    return o.Desc(case["kind"], case["buckets"], shift=case.get("shift", 0), param=case.get("param", 0),
+                  lower=case.get("lower", 0), inverse_delta=case.get("inverse_delta", 0.0), splitters=spl)
+
+
+def test_golden_inputs_regenerate(golden):
+    for case in golden:
+        assert sha(gen_keys(case)) == case["input_sha256"], case["name"]
+
+
+def test_oracle_matches_golden(golden, oracle_mod):
+    o = oracle_mod
+    for case in golden:
+        keys = gen_keys(case)
+        vals = np.arange(case["n"], dtype=np.uint32) if case["values"] else None
+        if case["op"] == "multisplit":
+            ko, vo, offs = o.multisplit(keys, desc_of(o, case), vals)
+            if "offsets" in case:
+                assert [int(x) for x in offs] == case["offsets"], case["name"]
+        elif case["op"] == "compaction":
+            ko, vo, n0 = o.compaction(keys, desc_of(o, case), vals)
+            assert n0 == case["num_bucket0"], case["name"]
+        elif case["op"] == "sort7":
+            ko, vo = o.sort_7bit(keys, vals)
+        else:
+            raise AssertionError(case["op"])
+        assert sha(ko) == case["keys_out_sha256"], case["name"]
+        if vals is not None:
+            assert sha(vo) == case["values_out_sha256"], case["name"]
+        if "keys_out" in case:
+            assert [int(x) for x in ko] == case["keys_out"], case["name"]
+
+
+def test_known_answer_delta_func(oracle_mod):
+    """keys 7 1 6 2 5 3 4 0, bucket a/2, B=4 -> 1 0 2 3 5 4 7 6 (reference CPU output)."""
+    o = oracle_mod
+    ko, _, offs = o.multisplit(np.array([7, 1, 6, 2, 5, 3, 4, 0], np.uint32), o.Desc(o.DIV, 4, param=2))
+    assert list(ko) == [1, 0, 2, 3, 5, 4, 7, 6]
+    assert list(offs) == [0, 2, 4, 6]
+
+
+def test_even_float_edges(oracle_mod):
+    """Float binning of the reference's even histogram (multisplit2_histograms.cuh:60):
+    keys >= 2^32-128 round to 2^32 -> bin 256 -> wraps to 0; 2^24-1 rounds exactly."""
+    o = oracle_mod
+    d = o.Desc(o.EVEN_FLOAT, 256, inverse_delta=2.0 ** -24)
+    keys = np.array([2**32 - 1, 2**32 - 128, 2**32 - 129, 2**24 - 1, 2**24, 2**25 - 1], np.uint32)
+    assert list(o.buckets(keys, d)) == [0, 0, 255, 0, 1, 2]
+
+
+def test_range_below_first_splitter_wraps(oracle_mod):
+    o = oracle_mod
+    d = o.Desc(o.RANGE, 4, splitters=np.array([10, 20, 30, 40], np.uint32))
+    assert list(o.buckets(np.array([0, 9, 10, 19, 20, 39, 40, 2**32 - 1], np.uint32), d)) == [3, 3, 0, 0, 1, 2, 3, 3]
+
+
+def test_tile_counts_layout(oracle_mod):
+    o = oracle_mod
+    keys = datagen.as_u32(datagen.uniform_u32(10000, 3))
+    d = o.Desc(o.DELTA, 16)
+    c = o.tile_counts(keys, d, 4096)
+    assert c.shape == (16, 3)
+    ids = keys >> np.uint32(28)
+    for t in range(3):
+        np.testing.assert_array_equal(c[:, t], np.bincount(ids[t * 4096:(t + 1) * 4096], minlength=16))
+
+
+def test_multithreaded_port_matches(oracle_mod):
+    o = oracle_mod
+    keys = datagen.as_u32(datagen.zipf_u32(200003, 4, distinct=1 << 10))
+    vals = np.arange(keys.size, dtype=np.uint32)
+    for d in (o.Desc(o.DELTA, 256), o.Desc(o.BITS, 2), o.Desc(o.DIV, 32, param=1 << 27)):
+        ko, vo, _ = o.multisplit(keys, d, vals)
+        mk, mv = o.multisplit_mt(keys, d, vals, threads=5)
+        assert np.array_equal(ko, mk) and np.array_equal(vo, mv)
+
+
+def test_sort_oracle_is_stable_sort(oracle_mod):
+    o = oracle_mod
+    keys = datagen.as_u32(datagen.and4_u32(50000, 9))
+    vals = np.arange(keys.size, dtype=np.uint32)
+    ko, vo = o.sort_7bit(keys, vals)
+    assert np.array_equal(ko, np.sort(keys))
+    assert np.array_equal(vo, np.argsort(keys, kind="stable"))
+
+
+@pytest.mark.skipif("not __import__('oracle').ref_available()", reason="reference CPU library not built here")
+def test_oracle_matches_reference_code(oracle_mod):
+    """Random cases: the C restatement equals the reference's own CPU multisplit."""
+    o = oracle_mod
+    rng = np.random.default_rng(0)
+    for trial in range(40):
+        B = int(2 ** rng.integers(1, 9))
+        n = int(rng.integers(0, 5000))
+        kind = int(rng.integers(0, 6))
+        keys = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+        vals = np.arange(n, dtype=np.uint32)
+        spl = np.sort(rng.integers(0, 2**32, B, dtype=np.uint64).astype(np.uint32))
+        d = o.Desc(kind, B, shift=int(rng.integers(0, 32)), param=int(rng.integers(1, 2**32)),
+                   lower=int(rng.integers(0, 2**32)), inverse_delta=float(B) / 2**32, splitters=spl)
+        ko, vo, _ = o.multisplit(keys, d, vals)
+        rk, rv = o.ref_multisplit(keys, d, vals)
+        assert np.array_equal(ko, rk) and np.array_equal(vo, rv), (trial, kind, B, n)
