@@ -37,18 +37,23 @@ from ._lib import BucketDesc, check
 # ---------------------------------------------------------------- helpers
 
 
-def _ptr(x) -> int | None:
+def _ptr(x, elem_bytes: int | None = 4) -> int | None:
+    """Device address of a CUDA tensor (of `elem_bytes`-byte elements) or an int."""
     if x is None:
         return None
     if isinstance(x, int):
         return x
     if hasattr(x, "data_ptr"):
-        if x.element_size() != 4:
+        if elem_bytes is not None and x.element_size() != elem_bytes:
             raise TypeError("multisplit buffers hold 32-bit elements")
         if not x.is_cuda:
             raise TypeError("multisplit buffers must be CUDA tensors")
         return x.data_ptr()
     raise TypeError(f"unsupported buffer type {type(x)!r}")
+
+
+def _scratch(ctx) -> int | None:
+    return _ptr(ctx.d_temp_storage, None)
 
 
 def _stream(stream=None) -> int | None:
@@ -60,9 +65,12 @@ def _stream(stream=None) -> int | None:
 
 
 def _alloc_scratch(nbytes: int):
+    """Scratch buffer; its 256-byte header (device error word, scan ticket) starts zeroed."""
     import torch
 
-    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device="cuda")
+    t = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device="cuda")
+    t[:256].zero_()
+    return t
 
 
 # ------------------------------------------------------ bucket identifiers
@@ -229,7 +237,7 @@ def multisplit_key_only(d_key_in, d_key_out, num_elements: int, context: multisp
     desc = bucket_identifier.desc(context.num_buckets)
     offs = _offsets_buffer(context.num_buckets) if multisplit_offset is not None else None
     check(_lib.load().gms_multisplit_key_only(_ptr(d_key_in), _ptr(d_key_out), num_elements, ctypes.byref(desc),
-                                              _ptr(context.d_temp_storage), context.temp_storage_bytes, offs,
+                                              _scratch(context), context.temp_storage_bytes, offs,
                                               _stream(stream)), "multisplit_key_only")
     return _export_offsets(offs, multisplit_offset)
 
@@ -241,7 +249,7 @@ def multisplit_key_value(d_key_in, d_value_in, d_key_out, d_value_out, num_eleme
     desc = bucket_identifier.desc(context.num_buckets)
     offs = _offsets_buffer(context.num_buckets) if multisplit_offset is not None else None
     check(_lib.load().gms_multisplit_key_value(_ptr(d_key_in), _ptr(d_value_in), _ptr(d_key_out), _ptr(d_value_out),
-                                               num_elements, ctypes.byref(desc), _ptr(context.d_temp_storage),
+                                               num_elements, ctypes.byref(desc), _scratch(context),
                                                context.temp_storage_bytes, offs, _stream(stream)),
           "multisplit_key_value")
     return _export_offsets(offs, multisplit_offset)
@@ -266,7 +274,7 @@ def multisplit_stages(d_key_in, d_value_in, d_key_out, d_value_out, num_elements
     desc = bucket_identifier.desc(context.num_buckets)
     kv = int(d_value_in is not None)
     s = _stream(stream)
-    scratch, nbytes = _ptr(context.d_temp_storage), context.temp_storage_bytes
+    scratch, nbytes = _scratch(context), context.temp_storage_bytes
     if events:
         events[0].record()
     check(lib.gms_multisplit_prescan(_ptr(d_key_in), num_elements, ctypes.byref(desc), kv, scratch, nbytes, s),
@@ -285,7 +293,7 @@ def multisplit_stages(d_key_in, d_value_in, d_key_out, d_value_out, num_elements
 def read_device_error(context, stream=None) -> int:
     """Device error word of a context's scratch (0 = every bounded wait finished)."""
     code = ctypes.c_uint32()
-    st = _lib.load().gms_read_device_error(_ptr(context.d_temp_storage), ctypes.byref(code), _stream(stream))
+    st = _lib.load().gms_read_device_error(_scratch(context), ctypes.byref(code), _stream(stream))
     if st not in (_lib.GMS_SUCCESS, _lib.GMS_ERROR_DEVICE_TIMEOUT):
         check(st, "read_device_error")
     return code.value
@@ -329,7 +337,7 @@ def multisplit_sort_release_memory(context: ms_sort_context) -> None:
 def multisplit_sort_7bit(d_key_in, d_key_out_ms, n_elements: int, context: ms_sort_context, stream=None) -> None:
     """src/api/multisplit_sort.cuh:320-364."""
     check(_lib.load().gms_sort_7bit_key_only(_ptr(d_key_in), _ptr(d_key_out_ms), n_elements,
-                                             _ptr(context.d_temp_storage), context.temp_storage_bytes,
+                                             _scratch(context), context.temp_storage_bytes,
                                              _stream(stream)), "multisplit_sort_7bit")
 
 
@@ -337,7 +345,7 @@ def multisplit_sort_7bit_pairs(d_key_in, d_key_out_ms, d_value_in, d_value_out_m
                                context: ms_sort_context, stream=None) -> None:
     """src/api/multisplit_sort_pairs.cuh:21-65 (argument order kin, kout, vin, vout)."""
     check(_lib.load().gms_sort_7bit_key_value(_ptr(d_key_in), _ptr(d_key_out_ms), _ptr(d_value_in),
-                                              _ptr(d_value_out_ms), n_elements, _ptr(context.d_temp_storage),
+                                              _ptr(d_value_out_ms), n_elements, _scratch(context),
                                               context.temp_storage_bytes, _stream(stream)),
           "multisplit_sort_7bit_pairs")
 
@@ -382,7 +390,7 @@ def compaction_key_only(d_key_in, d_key_out, num_elements: int, context: compact
     desc = bucket_identifier.desc(2)
     n0 = ctypes.c_uint32()
     check(_lib.load().gms_compaction_key_only(_ptr(d_key_in), _ptr(d_key_out), num_elements, ctypes.byref(desc),
-                                              _ptr(context.d_temp_storage), context.temp_storage_bytes,
+                                              _scratch(context), context.temp_storage_bytes,
                                               ctypes.byref(n0), _stream(stream)), "compaction_key_only")
     return n0.value
 
@@ -393,7 +401,7 @@ def compaction_key_value(d_key_in, d_value_in, d_key_out, d_value_out, num_eleme
     desc = bucket_identifier.desc(2)
     n0 = ctypes.c_uint32()
     check(_lib.load().gms_compaction_key_value(_ptr(d_key_in), _ptr(d_value_in), _ptr(d_key_out), _ptr(d_value_out),
-                                               num_elements, ctypes.byref(desc), _ptr(context.d_temp_storage),
+                                               num_elements, ctypes.byref(desc), _scratch(context),
                                                context.temp_storage_bytes, ctypes.byref(n0), _stream(stream)),
           "compaction_key_value")
     return n0.value

@@ -184,9 +184,9 @@ def test_errors_are_reported(gms_lib):
         gms.multisplit_allocate_key_only(100, ctx)
     ctx = gms.multisplit_context(16)
     gms.multisplit_allocate_key_only(1000, ctx)
-    dk = torch.zeros(5000, dtype=torch.int32, device="cuda")
+    dk = torch.zeros(100000, dtype=torch.int32, device="cuda")
     ok = torch.zeros_like(dk)
     with pytest.raises(gms.GmsError):  # over the context's capacity
-        gms.multisplit_key_only(dk, ok, 5000, ctx, gms.delta_bucket())
+        gms.multisplit_key_only(dk, ok, 100000, ctx, gms.delta_bucket())
     with pytest.raises(gms.GmsError):  # in place is not supported
         gms.multisplit_key_only(dk, dk, 1000, ctx, gms.delta_bucket())
