@@ -236,6 +236,8 @@ cudaError_t run_scan(uint32_t* data, uint32_t m, uint64_t* status, ScratchHeader
   return cudaGetLastError();
 }
 
+void note_cuda_error(cudaError_t e) { g_last_cuda_error = int(e); }
+
 int device_sm_count() {
   static std::atomic<int> cached[64];
   int dev = 0;

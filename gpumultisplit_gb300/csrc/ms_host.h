@@ -78,4 +78,7 @@ cudaError_t run_scan(uint32_t* data, uint32_t m, uint64_t* status, ScratchHeader
 
 int device_sm_count();
 
+// Records a CUDA error for gms_last_cuda_error() (calling thread).
+void note_cuda_error(cudaError_t e);
+
 }  // namespace gms

@@ -127,6 +127,23 @@ gms_status gms_multisplit_postscan(const uint32_t* d_key_in, const uint32_t* d_v
 gms_status gms_multisplit_geometry(uint32_t n, uint32_t num_buckets, int key_value, uint32_t* tile_keys,
                                    uint32_t* num_tiles, size_t* matrix_offset_bytes);
 
+/* Key-value multisplit that allocates nothing.  No counterpart in the reference:
+ * it exists for callers that cannot call cudaMalloc where they need a multisplit
+ * (allocator internals, plugin hosts that hand over only input and output
+ * buffers, paths that must not allocate after start-up).  Its scratch is a fixed
+ * GMS_NOALLOC_SCRATCH_BYTES array in device memory owned by the library (held on
+ * every GPU that loads the library until the process exits).  Calls that need
+ * more scratch than that (gms_multisplit_scratch_bytes(n, B, 1) > the limit:
+ * about 16 M pairs at 256 buckets) return GMS_ERROR_SCRATCH_TOO_SMALL.  The
+ * first call on a device looks up the array's address with that device
+ * current; make it before any stream capture.  All calls on a device share the
+ * array, so calls that overlap on the GPU race; each call resets what it reads.
+ * Output is identical to gms_multisplit_key_value (no bucket offsets). */
+#define GMS_NOALLOC_SCRATCH_BYTES (4u << 20)
+gms_status gms_multisplit_key_value_noalloc(const uint32_t* d_key_in, const uint32_t* d_value_in,
+                                            uint32_t* d_key_out, uint32_t* d_value_out, uint32_t n,
+                                            const gms_bucket_desc* desc, gms_stream_t stream);
+
 /* ----------------------------------------------------------------- sort */
 /* Replaces multisplit_sort_7bit_allocate / _allocate_pairs (src/api/multisplit_sort.cuh:151-191).
  * Includes the ping-pong key (and value) buffer the reference keeps in d_key_temp_ms. */
