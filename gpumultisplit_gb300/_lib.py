@@ -96,7 +96,8 @@ def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = Path(path) if path is not None else LIB_PATH
+    override = os.environ.get("GMS_LIBRARY")
+    p = Path(path) if path is not None else (Path(override) if override else LIB_PATH)
     if not p.exists():
         raise ImportError(
             f"{p} is missing: build the CUDA library first "

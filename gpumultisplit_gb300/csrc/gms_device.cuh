@@ -98,6 +98,12 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
       : "memory");
 }
 
+// Prefetch [src, src + bytes) into L2 (no completion tracking); src 16-byte
+// aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ void st_relaxed_u64(uint64_t* p, uint64_t v) {
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
@@ -144,8 +150,20 @@ struct BucketParams {
   const uint32_t* splitters;  // RANGE only (device memory, B entries)
 };
 
-// A bucket identifier for B = 2^LOGB buckets.  `s_split` is a shared-memory
-// copy of the splitters (RANGE only), filled by load_splitters().
+// RANGE identifiers narrow each search with a table over the key's top
+// RANGE_LUT_BITS bits: lut[t] = number of splitters below t << (32 - bits),
+// so a key in cell t has between lut[t] and lut[t+1] splitters <= it.
+constexpr int RANGE_LUT_BITS = 8;
+constexpr uint32_t RANGE_LUT_CELLS = 1u << RANGE_LUT_BITS;
+
+// Shared words an identifier needs (splitters + lookup table for RANGE).
+template <int KIND, int LOGB>
+__host__ __device__ constexpr uint32_t identifier_smem_words() {
+  return KIND == KIND_RANGE ? (1u << LOGB) + (RANGE_LUT_CELLS + 2) / 2 : 1u;
+}
+
+// A bucket identifier for B = 2^LOGB buckets.  `s_split` is the shared-memory
+// area filled by prepare_identifier() (RANGE only).
 template <int KIND, int LOGB>
 struct Identifier {
   static constexpr uint32_t B = 1u << LOGB;
@@ -161,14 +179,19 @@ struct Identifier {
     } else if constexpr (KIND == KIND_BITS) {
       return (key >> p.shift) & (B - 1);
     } else if constexpr (KIND == KIND_RANGE) {
-      // Largest i with s[i] <= key (= upper_bound - 1); -1 (wrapped to B-1)
-      // when key < s[0].  Branch-free binary search over B sorted splitters.
-      uint32_t pos = 0;
-#pragma unroll
-      for (uint32_t step = B >> 1; step >= 1; step >>= 1) {
-        pos += (s_split[pos + step] <= key) ? step : 0u;
+      // c = number of splitters <= key (upper_bound); bucket = c - 1, which
+      // wraps to B-1 when key < s[0].  The table bounds c to [lut[t], lut[t+1]].
+      const uint16_t* lut = reinterpret_cast<const uint16_t*>(s_split + B);
+      const uint32_t t = key >> (32 - RANGE_LUT_BITS);
+      uint32_t c = lut[t], hi = lut[t + 1];
+      while (c < hi) {
+        const uint32_t mid = (c + hi + 1) >> 1;
+        if (s_split[mid - 1] <= key)
+          c = mid;
+        else
+          hi = mid - 1;
       }
-      return (key < s_split[0]) ? (B - 1) : pos;
+      return (c - 1u) & (B - 1);
     } else if constexpr (KIND == KIND_MASK) {
       return (key & p.param) ? 1u : 0u;
     } else {  // KIND_EVEN_FLOAT
@@ -178,11 +201,31 @@ struct Identifier {
   }
 };
 
-// Copy the RANGE splitters into shared memory (no-op for other kinds).
+// Fill the identifier's shared area (RANGE: splitters, then the lookup table).
+// No-op for other kinds.  All threads of the block must call it.
 template <int KIND, int LOGB>
-__device__ __forceinline__ void load_splitters(uint32_t* s_split, const BucketParams& p) {
+__device__ __forceinline__ void prepare_identifier(uint32_t* s_split, const BucketParams& p) {
   if constexpr (KIND == KIND_RANGE) {
-    for (uint32_t i = threadIdx.x; i < (1u << LOGB); i += blockDim.x) s_split[i] = p.splitters[i];
+    constexpr uint32_t B = 1u << LOGB;
+    for (uint32_t i = threadIdx.x; i < B; i += blockDim.x) s_split[i] = p.splitters[i];
+    __syncthreads();
+    uint16_t* lut = reinterpret_cast<uint16_t*>(s_split + B);
+    for (uint32_t t = threadIdx.x; t <= RANGE_LUT_CELLS; t += blockDim.x) {
+      uint32_t lo = B;  // lower_bound of t << (32 - bits); the top cell ends at 2^32
+      if (t < RANGE_LUT_CELLS) {
+        const uint32_t v = t << (32 - RANGE_LUT_BITS);
+        uint32_t hi = B;
+        lo = 0;
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (s_split[mid] < v)
+            lo = mid + 1;
+          else
+            hi = mid;
+        }
+      }
+      lut[t] = uint16_t(lo);
+    }
   }
 }
 

@@ -26,6 +26,26 @@ inline cudaError_t ensure_smem_limit(Kernel k, size_t bytes, std::atomic<uint64_
   return e;
 }
 
+// Grid of a persistent kernel: as many blocks as fit on the device at once
+// (cached per kernel; the device's SM count is read per call), capped by `work`.
+// Postscan L2 prefetch distance, in quarters of a wave of resident blocks (0 = off).
+#ifndef GMS_PREFETCH_WAVES
+#define GMS_PREFETCH_WAVES 2
+#endif
+
+template <class Kernel>
+inline uint32_t persistent_grid(Kernel k, int threads, uint32_t work, std::atomic<int>& per_sm_cache,
+                                size_t smem = 0) {
+  int per_sm = per_sm_cache.load(std::memory_order_relaxed);
+  if (per_sm <= 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem) != cudaSuccess || per_sm <= 0)
+      per_sm = 1;
+    per_sm_cache.store(per_sm, std::memory_order_relaxed);
+  }
+  const uint64_t cap = uint64_t(device_sm_count()) * uint64_t(per_sm);
+  return uint32_t(work < cap ? work : cap);
+}
+
 template <int KIND, int LOGB, bool KV>
 cudaError_t run_multisplit_t(const MsCall& c, int stages) {
   using S = TileShape<LOGB, KV>;
@@ -37,8 +57,10 @@ cudaError_t run_multisplit_t(const MsCall& c, int stages) {
   auto* matrix = reinterpret_cast<uint32_t*>(c.scratch + g.off_matrix);
 
   if (stages & STAGE_PRESCAN) {
-    prescan_kernel<C, KIND><<<g.num_tiles, C::THREADS, 0, c.stream>>>(c.kin, c.n, g.num_tiles, matrix, c.bp, hdr,
-                                                                      status, g.num_chunks);
+    static std::atomic<int> per_sm{0};
+    auto kern = prescan_kernel<C, KIND>;
+    const uint32_t grid = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm);
+    kern<<<grid, C::THREADS, 0, c.stream>>>(c.kin, c.n, g.num_tiles, matrix, c.bp, hdr, status, g.num_chunks);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -48,11 +70,16 @@ cudaError_t run_multisplit_t(const MsCall& c, int stages) {
   }
   if (stages & STAGE_POSTSCAN) {
     static std::atomic<uint64_t> smem_done{0};
+    static std::atomic<int> per_sm{0};
     auto kern = postscan_kernel<C, KIND>;
-    cudaError_t e = ensure_smem_limit(kern, C::POST_SMEM, smem_done);
+    constexpr size_t smem = PostLayout<C, KIND>::BYTES;
+    cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
     if (e != cudaSuccess) return e;
-    kern<<<g.num_tiles, C::THREADS, C::POST_SMEM, c.stream>>>(c.kin, c.vin, c.kout, c.vout, c.n, g.num_tiles, matrix,
-                                                             c.bp, hdr);
+    // Prefetch distance: the number of blocks resident at once (one wave).
+    const uint32_t wave = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
+    const uint32_t dist = (GMS_PREFETCH_WAVES * wave) / 4u;
+    kern<<<g.num_tiles, C::THREADS, smem, c.stream>>>(c.kin, c.vin, c.kout, c.vout, c.n, g.num_tiles, matrix,
+                                                             c.bp, hdr, dist);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -83,10 +110,10 @@ template <int KIND, int LOGB>
 cudaError_t run_histogram_t(const uint32_t* keys, uint32_t n, const BucketParams& bp, int32_t* hist,
                             cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
-  const uint32_t chunks = (n + HIST_CHUNK - 1) / HIST_CHUNK;
-  const uint32_t cap = uint32_t(device_sm_count()) * 8u;
-  const uint32_t grid = chunks < cap ? chunks : cap;
-  histogram_kernel<LOGB, KIND><<<grid, HIST_THREADS, 0, stream>>>(keys, n, hist, bp);
+  static std::atomic<int> per_sm{0};
+  auto kern = histogram_kernel<LOGB, KIND>;
+  const uint32_t grid = persistent_grid(kern, HIST_THREADS, (n + HIST_CHUNK - 1) / HIST_CHUNK, per_sm);
+  kern<<<grid, HIST_THREADS, 0, stream>>>(keys, n, hist, bp);
   return cudaGetLastError();
 }
 

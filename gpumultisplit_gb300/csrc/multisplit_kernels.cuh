@@ -17,6 +17,18 @@
 
 #include "gms_device.cuh"
 
+// How a warp finds, for B > 32, the lanes holding the same bucket as each lane
+// (its peer mask) in one 32-key slot:
+//   0  log2(B) bit-plane ballots (logic pipe);
+//   1  match.any (one instruction on its own pipe, but about 1.6x slower here);
+//   2  a shared-memory atomicOr of each lane's bit into a per-warp bitmap
+//      indexed by bucket, then one load (OR is order-independent, so the mask
+//      is deterministic); it trades logic work for shared-memory traffic and
+//      measured about 7% slower.
+#ifndef GMS_PEERS_MODE
+#define GMS_PEERS_MODE 0
+#endif
+
 namespace gms {
 
 // Tile geometry of one (B, key/value) instance.
@@ -30,133 +42,404 @@ struct TileCfg {
   static constexpr uint32_t TILE = THREADS * IPT_;
   static constexpr bool KV = KV_;
   static constexpr uint32_t WB = B < 32 ? 32 : B;  // row width of the per-warp count table
+  // Words per count-table entry: {peer bitmap, count} pairs when the bitmap
+  // peer search is used (B > 32), else the count alone.
+  static constexpr uint32_t WS = (LOGB_ > 5 && GMS_PEERS_MODE == 2) ? 2 : 1;
 
   static_assert(IPT % 4 == 0, "IPT must be a multiple of 4 (16-byte vector loads)");
   static_assert(TILE <= 65536, "in-tile positions are packed into 16 bits");
   static_assert(THREADS >= static_cast<int>(B), "one thread per bucket in the tile scan");
 
-  // Postscan shared-memory layout (bytes).
-  static constexpr size_t OFF_K = 0;
-  static constexpr size_t OFF_V = OFF_K + TILE * 4;
-  static constexpr size_t OFF_R = OFF_V + (KV ? TILE * 4 : 0);
-  static constexpr size_t OFF_WH = OFF_R + TILE * 4;
-  static constexpr size_t OFF_DELTA = OFF_WH + size_t(WARPS) * WB * 4;
-  static constexpr size_t OFF_SPLIT = OFF_DELTA + B * 4;
-  static constexpr size_t OFF_SCAN = OFF_SPLIT + B * 4;
-  static constexpr size_t OFF_BAR = (OFF_SCAN + B * 4 + 15) & ~size_t(15);
-  static constexpr size_t POST_SMEM = OFF_BAR + 16;
 };
 
 // ------------------------------------------------------------- counting
-// Counts keys into per-lane registers (B <= 32: lane l counts bucket l, from
-// log2(B) ballots per 32 keys) or into a shared histogram (B > 32).
+// Counting keys per bucket.  For the smallest bucket counts every lane keeps
+// the count of bucket `lane` in registers, fed by log2(B) ballots per 32 keys;
+// otherwise keys are counted with shared-memory atomics into R replicas of a
+// B-entry histogram (R = 32/B below 32 buckets, lane l using replica l % R), so
+// few lanes of a warp ever hit the same word.
+#ifndef GMS_COUNT_BALLOT_MAX_LOGB
+#define GMS_COUNT_BALLOT_MAX_LOGB 0
+#endif
+
 template <int LOGB, int KIND>
 struct KeyCounter {
   static constexpr uint32_t B = 1u << LOGB;
-  static constexpr bool kBallot = LOGB <= 5;
+  static constexpr bool kBallot = LOGB <= GMS_COUNT_BALLOT_MAX_LOGB;
+  static constexpr uint32_t R = B >= 32 ? 1u : 32u / B;  // histogram replicas (atomic path)
+  static constexpr uint32_t HIST_WORDS = B * R;         // >= 32
   Identifier<KIND, LOGB> ident;
-  uint32_t* s_hist;  // B > 32
-  uint32_t lane_cnt = 0;
-  uint32_t xm[LOGB <= 5 ? LOGB : 1];
+  uint32_t* s_hist;                      // HIST_WORDS (atomic path) or WARPS*32 (ballot path)
+  uint32_t acc[4] = {0u, 0u, 0u, 0u};    // ballot path: independent accumulators keep the chains parallel
+  uint32_t xm[kBallot ? LOGB : 1];
+  uint32_t slot;                          // atomic path: this lane's replica offset
 
   __device__ __forceinline__ KeyCounter(const Identifier<KIND, LOGB>& id, uint32_t* hist) : ident(id), s_hist(hist) {
+    const uint32_t lane = lane_id();
     if constexpr (kBallot) {
-      const uint32_t lane = lane_id();
 #pragma unroll
       for (int i = 0; i < LOGB; ++i) xm[i] = ((lane >> i) & 1u) ? 0u : ~0u;
     }
+    slot = lane & (R - 1);
   }
 
-  // Called by all 32 lanes of the warp together.
+  // Called by all 32 lanes of the warp together; A selects an accumulator.
+  template <int A = 0>
   __device__ __forceinline__ void add(uint32_t key, bool valid) {
     const uint32_t b = ident(key);
     if constexpr (kBallot) {
       uint32_t m = __ballot_sync(~0u, valid);
 #pragma unroll
       for (int i = 0; i < LOGB; ++i) m &= __ballot_sync(~0u, (b >> i) & 1u) ^ xm[i];
-      lane_cnt += __popc(m);
+      acc[A] += __popc(m);
     } else {
-      if (valid) atomicAdd(&s_hist[b], 1u);
+      if (valid) atomicAdd(&s_hist[b * R + slot], 1u);
     }
+  }
+
+  // Shared words the counter needs for a block of `warps` warps.
+  __host__ __device__ static constexpr uint32_t smem_words(int warps) { return kBallot ? uint32_t(warps) * 32u : HIST_WORDS; }
+
+  // Zero the shared histogram (atomic path); all threads call, a barrier must follow.
+  __device__ __forceinline__ void clear_shared() {
+    if constexpr (!kBallot) {
+      for (uint32_t i = threadIdx.x; i < HIST_WORDS; i += blockDim.x) s_hist[i] = 0u;
+    }
+  }
+
+  // Block totals: after the call (which contains barriers), thread b < B returns
+  // the block's count of bucket b, and the counter is reset for the next tile.
+  __device__ __forceinline__ uint32_t block_total() {
+    const uint32_t tid = threadIdx.x;
+    uint32_t total = 0;
+    if constexpr (kBallot) {
+      const uint32_t lane = tid & 31u, warp = tid >> 5;
+      if (lane < B) s_hist[warp * 32 + lane] = acc[0] + acc[1] + acc[2] + acc[3];
+      acc[0] = acc[1] = acc[2] = acc[3] = 0u;
+      __syncthreads();
+      if (tid < B) {
+        for (uint32_t w = 0; w < blockDim.x / 32; ++w) total += s_hist[w * 32 + tid];
+      }
+      __syncthreads();
+    } else {
+      __syncthreads();
+      if (tid < B) {
+#pragma unroll
+        for (uint32_t r = 0; r < R; ++r) {
+          total += s_hist[tid * R + r];
+          s_hist[tid * R + r] = 0u;
+        }
+      }
+      __syncthreads();
+    }
+    return total;
   }
 };
 
-// Count the keys keys[base .. base+cnt) of one tile of THREADS*IPT keys.
-template <int THREADS, int IPT, class Counter>
-__device__ __forceinline__ void count_tile(const uint32_t* __restrict__ keys, uint32_t base, uint32_t cnt,
-                                           bool vec_ok, Counter& c) {
-  const uint32_t tid = threadIdx.x;
-  if (vec_ok && cnt == uint32_t(THREADS * IPT)) {
-    uint4 v[IPT / 4];
+template <int THREADS, int IPT>
+__device__ __forceinline__ void load_tile_v4(const uint32_t* __restrict__ keys, uint32_t base, uint4 (&v)[IPT / 4]) {
 #pragma unroll
-    for (int k = 0; k < IPT / 4; ++k) v[k] = ld_nc_v4(keys + base + (uint32_t(k) * THREADS + tid) * 4u);
+  for (int k = 0; k < IPT / 4; ++k) v[k] = ld_nc_v4(keys + base + (uint32_t(k) * THREADS + threadIdx.x) * 4u);
+}
+
+template <int IPT, class Counter>
+__device__ __forceinline__ void count_v4(const uint4 (&v)[IPT / 4], Counter& c) {
 #pragma unroll
-    for (int k = 0; k < IPT / 4; ++k) {
-      c.add(v[k].x, true);
-      c.add(v[k].y, true);
-      c.add(v[k].z, true);
-      c.add(v[k].w, true);
-    }
-  } else {
+  for (int k = 0; k < IPT / 4; ++k) {
+    c.template add<0>(v[k].x, true);
+    c.template add<1>(v[k].y, true);
+    c.template add<2>(v[k].z, true);
+    c.template add<3>(v[k].w, true);
+  }
+}
+
+// Counts tiles first, first+stride, ... (tiles of THREADS*IPT keys) and calls
+// done(tile) after each one.  The next tile's keys are loaded into registers
+// while the current tile is counted, so loads stay in flight.
+template <int THREADS, int IPT, class Counter, class Done>
+__device__ __forceinline__ void count_tiles(const uint32_t* __restrict__ keys, uint32_t n, uint32_t first,
+                                            uint32_t stride, Counter& c, Done done) {
+  constexpr uint32_t TILE = uint32_t(THREADS) * IPT;
+  const uint32_t num_tiles = uint32_t((uint64_t(n) + TILE - 1) / TILE);
+  const bool vec_ok = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0;
+  const uint32_t full_tiles = vec_ok ? n / TILE : 0u;  // tiles read with vector loads
+  uint4 cur[IPT / 4];
+  if (first < full_tiles) load_tile_v4<THREADS, IPT>(keys, first * TILE, cur);
+  for (uint32_t tile = first; tile < num_tiles; tile += stride) {
+    const uint32_t next = tile + stride;
+    uint4 nxt[IPT / 4];
+    if (next < full_tiles) load_tile_v4<THREADS, IPT>(keys, next * TILE, nxt);
+    if (tile < full_tiles) {
+      count_v4<IPT>(cur, c);
+    } else {
+      const uint32_t base = tile * TILE;
+      const uint32_t cnt = min(TILE, n - base);
 #pragma unroll 4
-    for (int k = 0; k < IPT; ++k) {
-      const uint32_t i = uint32_t(k) * THREADS + tid;
-      const bool valid = i < cnt;
-      const uint32_t key = valid ? keys[base + i] : 0u;
-      c.add(key, valid);
+      for (int k = 0; k < IPT; ++k) {
+        const uint32_t i = uint32_t(k) * THREADS + threadIdx.x;
+        const bool valid = i < cnt;
+        c.add(valid ? keys[base + i] : 0u, valid);
+      }
     }
+    done(tile);
+#pragma unroll
+    for (int k = 0; k < IPT / 4; ++k) cur[k] = nxt[k];
   }
 }
 
 // --------------------------------------------------------------- prescan
-// One CTA per tile.  Writes counts[b * num_tiles + tile] and resets the scan
-// state (ticket, chunk status words, error word) for the scan that follows.
+// Persistent grid over the tiles.  Writes counts[b * num_tiles + tile] for
+// every tile and resets the scan state (ticket, chunk status words, error
+// word) for the scan that follows.
 template <class C, int KIND>
 __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __restrict__ keys, uint32_t n,
                                                              uint32_t num_tiles, uint32_t* __restrict__ counts,
                                                              BucketParams bp, ScratchHeader* hdr,
                                                              uint64_t* __restrict__ status, uint32_t num_chunks) {
-  constexpr uint32_t B = C::B;
-  __shared__ uint32_t s_hist[C::LOGB <= 5 ? C::WARPS * 32 : B];
-  __shared__ uint32_t s_split[C::LOGB <= 5 ? 32 : B];  // RANGE splitters
+  using Counter = KeyCounter<C::LOGB, KIND>;
+  __shared__ uint32_t s_hist[Counter::smem_words(C::WARPS)];
+  __shared__ uint32_t s_split[identifier_smem_words<KIND, C::LOGB>()];  // RANGE splitters + table
 
   const uint32_t tid = threadIdx.x;
-  const uint32_t tile = blockIdx.x;
 
   // Reset the scan state for this call.
-  for (uint32_t i = tile * C::THREADS + tid; i < num_chunks; i += gridDim.x * C::THREADS) status[i] = 0ull;
-  if (tile == 0 && tid == 0) {
+  for (uint32_t i = blockIdx.x * C::THREADS + tid; i < num_chunks; i += gridDim.x * C::THREADS) status[i] = 0ull;
+  if (blockIdx.x == 0 && tid == 0) {
     hdr->error = 0u;
     hdr->error_info = 0u;
     hdr->ticket = 0u;
   }
 
-  load_splitters<KIND, C::LOGB>(s_split, bp);
-  if constexpr (C::LOGB > 5) {
-    for (uint32_t b = tid; b < B; b += C::THREADS) s_hist[b] = 0u;
+  prepare_identifier<KIND, C::LOGB>(s_split, bp);
+  Identifier<KIND, C::LOGB> ident{bp, s_split};
+  Counter counter(ident, s_hist);
+  counter.clear_shared();
+  __syncthreads();
+  count_tiles<C::THREADS, C::IPT>(keys, n, blockIdx.x, gridDim.x, counter, [&](uint32_t tile) {
+    const uint32_t total = counter.block_total();
+    if (tid < C::B) counts[tid * num_tiles + tile] = total;
+  });
+}
+
+// Shared-memory layout of the postscan for identifier KIND (bytes), and what
+// phase 3 writes into the reorder buffer R at each key's bucket-sorted position:
+//   R_KEYS     the key itself (key-only, identifier cheap to recompute): phase 4
+//              reads keys conflict-free and recomputes their buckets;
+//   R_INDEX16  the key's 16-bit in-tile index (key-value, cheap identifier):
+//              a small buffer keeps four tiles resident per SM;
+//   R_PACKED   (bucket << 16) | index, for identifiers that are costly to
+//              recompute (RANGE, DIV, EVEN_FLOAT).
+enum ReorderMode { R_KEYS = 0, R_INDEX16 = 1, R_PACKED = 2 };
+
+template <class C, int KIND>
+struct PostLayout {
+  static constexpr bool CHEAP = KIND == KIND_DELTA || KIND == KIND_BITS || KIND == KIND_MASK;
+  static constexpr int MODE = !CHEAP ? R_PACKED : (C::KV ? R_INDEX16 : R_KEYS);
+  static constexpr size_t OFF_K = 0;
+  static constexpr size_t OFF_V = OFF_K + C::TILE * 4;
+  static constexpr size_t OFF_R = OFF_V + (C::KV ? C::TILE * 4 : 0);
+  static constexpr size_t R_BYTES = size_t(C::TILE) * (MODE == R_INDEX16 ? 2 : 4);
+  static constexpr size_t OFF_WH = (OFF_R + R_BYTES + 15) & ~size_t(15);
+  static constexpr size_t OFF_DELTA = OFF_WH + size_t(C::WARPS) * C::WB * C::WS * 4;
+  static constexpr size_t OFF_SPLIT = OFF_DELTA + C::B * 4;
+  static constexpr size_t OFF_SCAN = OFF_SPLIT + identifier_smem_words<KIND, C::LOGB>() * 4;
+  static constexpr size_t OFF_FLAG = OFF_SCAN + C::B * 4;
+  static constexpr size_t OFF_BAR = (OFF_FLAG + 4 + 15) & ~size_t(15);
+  static constexpr size_t BYTES = OFF_BAR + 16;
+  // Blocks per SM the register budget is sized for (64 registers at 16 keys per thread).
+  static constexpr int MIN_BLOCKS = (C::IPT <= 8 ? 1536 : 1024) / C::THREADS > 0 ? (C::IPT <= 8 ? 1536 : 1024) / C::THREADS : 1;
+};
+
+// Peer mask (lanes of this warp whose key in this slot has bucket b) from
+// log2(B) bit-plane ballots: lanes agree on bit i iff ballot_i ^ own_i is set,
+// with own_i = 0 or ~0 by this lane's bit i.
+template <int LOGB>
+__device__ __forceinline__ uint32_t peers_by_ballot(uint32_t b) {
+  uint32_t peers = ~0u;
+#pragma unroll
+  for (int i = 0; i < LOGB; ++i) {
+    const uint32_t bal = __ballot_sync(~0u, (b >> i) & 1u);
+    const uint32_t own = ((b >> i) & 1u) - 1u;  // bit set -> 0, clear -> ~0
+    peers &= bal ^ own;
+  }
+  return peers;
+}
+
+// Phases 1-4 of the postscan for one staged tile.  FULL: the tile holds
+// exactly TILE keys, so no per-key validity test is needed.
+template <class C, int KIND, bool FULL>
+__device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
+                                              uint32_t cnt, uint32_t goff, const BucketParams& bp, ScratchHeader* hdr,
+                                              unsigned char* smem) {
+  using L = PostLayout<C, KIND>;
+  constexpr uint32_t B = C::B;
+  constexpr int LOGB = C::LOGB;
+  constexpr int IPT = C::IPT;
+  constexpr uint32_t WB = C::WB;
+  constexpr uint32_t WS = C::WS;
+  uint32_t* s_k = reinterpret_cast<uint32_t*>(smem + L::OFF_K);
+  uint32_t* s_v = reinterpret_cast<uint32_t*>(smem + L::OFF_V);
+  uint32_t* s_r = reinterpret_cast<uint32_t*>(smem + L::OFF_R);
+  uint32_t* s_wh = reinterpret_cast<uint32_t*>(smem + L::OFF_WH);
+  uint32_t* s_delta = reinterpret_cast<uint32_t*>(smem + L::OFF_DELTA);
+  const uint32_t* s_split = reinterpret_cast<const uint32_t*>(smem + L::OFF_SPLIT);
+  uint32_t* s_scan = reinterpret_cast<uint32_t*>(smem + L::OFF_SCAN);
+  uint32_t* s_flag = reinterpret_cast<uint32_t*>(smem + L::OFF_FLAG);
+  const uint32_t tid = threadIdx.x;
+  const uint32_t lane = tid & 31u;
+  const uint32_t warp = tid >> 5;
+
+  // ---- 1. stable in-warp ranks
+  const Identifier<KIND, LOGB> ident{bp, s_split};
+  uint32_t packed[IPT];  // (bucket << 16) | rank among same-bucket keys of this warp
+  const uint32_t wbase = warp * (IPT * 32u);
+  const uint32_t lt = lanemask_lt();
+  if constexpr (LOGB <= 5) {
+    // Lane l counts bucket l: its mask of lanes holding bucket l comes straight
+    // from the ballots, and a key's peers and earlier count are read from the
+    // lane that owns its bucket.
+    uint32_t xm[LOGB];
+#pragma unroll
+    for (int i = 0; i < LOGB; ++i) xm[i] = ((lane >> i) & 1u) ? 0u : ~0u;
+    uint32_t my_cnt = 0;
+#pragma unroll
+    for (int j = 0; j < IPT; ++j) {
+      const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
+      const uint32_t b = ident(s_k[pos]);
+      uint32_t m = FULL ? ~0u : __ballot_sync(~0u, pos < cnt);
+#pragma unroll
+      for (int i = 0; i < LOGB; ++i) m &= __ballot_sync(~0u, (b >> i) & 1u) ^ xm[i];
+      const uint32_t peers = __shfl_sync(~0u, m, b);
+      const uint32_t before = __shfl_sync(~0u, my_cnt, b);
+      packed[j] = (b << 16) | (before + __popc(peers & lt));
+      my_cnt += __popc(m);
+    }
+    if (lane < B) s_wh[warp * WB + lane] = my_cnt;
+  } else {
+    uint32_t* wh = s_wh + warp * WB * WS;  // entry b: count at [b*WS + WS-1], bitmap at [b*WS] when WS == 2
+    if constexpr (GMS_PEERS_MODE == 2) {
+#pragma unroll
+      for (int j = 0; j < IPT; ++j) {
+        const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
+        const bool valid = FULL || pos < cnt;
+        const uint32_t b = ident(s_k[pos]);
+        uint32_t* e = &wh[b * WS];
+        if (valid) atomicOr(e, 1u << lane);
+        __syncwarp();
+        const uint2 v = *reinterpret_cast<const uint2*>(e);
+        const uint32_t rank = __popc(v.x & lt);
+        __syncwarp();
+        if (valid && rank == 0) *reinterpret_cast<uint2*>(e) = make_uint2(0u, v.y + __popc(v.x));
+        __syncwarp();
+        packed[j] = (b << 16) | (v.y + rank);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < IPT; ++j) {
+        const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
+        const bool valid = FULL || pos < cnt;
+        const uint32_t b = ident(s_k[pos]);
+#if GMS_PEERS_MODE == 1
+        uint32_t peers = __match_any_sync(~0u, b);
+#else
+        uint32_t peers = peers_by_ballot<LOGB>(b);
+#endif
+        if (!FULL) peers &= __ballot_sync(~0u, valid);
+        const uint32_t rank = __popc(peers & lt);
+        uint32_t* e = &wh[b * WS + (WS - 1)];
+        const uint32_t before = *e;
+        __syncwarp();
+        if (valid && rank == 0) *e = before + __popc(peers);
+        __syncwarp();
+        packed[j] = (b << 16) | (before + rank);
+      }
+    }
   }
   __syncthreads();
 
-  const uint32_t base = tile * C::TILE;
-  const uint32_t cnt = min(C::TILE, n - base);
-  const bool vec_ok = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0;
-  Identifier<KIND, C::LOGB> ident{bp, s_split};
-  KeyCounter<C::LOGB, KIND> counter(ident, s_hist);
-  count_tile<C::THREADS, C::IPT>(keys, base, cnt, vec_ok, counter);
-
-  if constexpr (C::LOGB <= 5) {
-    const uint32_t lane = tid & 31u, warp = tid >> 5;
-    if (lane < B) s_hist[warp * 32 + lane] = counter.lane_cnt;
+  // ---- 2. tile scan: per-warp offsets, bucket starts, and a range check of
+  // every bucket's output run against n (a corrupt offset matrix can then never
+  // cause a store outside the output).  Thread b owns bucket b; the bucket
+  // starts come from a block-wide exclusive scan (warp scans + warp totals).
+  {
+    uint32_t total = 0;
+    if (tid < B) {
+#pragma unroll
+      for (int w = 0; w < C::WARPS; ++w) {
+        uint32_t* c_ptr = &s_wh[(w * WB + tid) * WS + (WS - 1)];
+        const uint32_t c = *c_ptr;
+        *c_ptr = total;
+        total += c;
+      }
+      if (uint64_t(goff) + total > n) atomicOr(s_flag, 1u);
+    }
+    uint32_t incl = total;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(~0u, incl, d);
+      if (lane >= uint32_t(d)) incl += t;
+    }
+    constexpr uint32_t SCAN_WARPS = (B + 31) / 32;
+    if (SCAN_WARPS > 1 && lane == 31 && warp < SCAN_WARPS) s_scan[warp] = incl;
     __syncthreads();
     if (tid < B) {
-      uint32_t total = 0;
+      uint32_t start = incl - total;
+      if constexpr (SCAN_WARPS > 1) {
 #pragma unroll
-      for (int w = 0; w < C::WARPS; ++w) total += s_hist[w * 32 + tid];
-      counts[tid * num_tiles + tile] = total;
+        for (uint32_t w = 0; w < SCAN_WARPS; ++w) start += (w < warp) ? s_scan[w] : 0u;
+      }
+      s_delta[tid] = goff - start;
+#pragma unroll
+      for (int w = 0; w < C::WARPS; ++w) s_wh[(w * WB + tid) * WS + (WS - 1)] += start;
     }
-  } else {
-    __syncthreads();
-    for (uint32_t b = tid; b < B; b += C::THREADS) counts[b * num_tiles + tile] = s_hist[b];
+  }
+  __syncthreads();
+  if (*s_flag != 0u) {  // block-uniform
+    if (tid == 0) record_error(hdr, DEV_ERR_BAD_OFFSET);
+    return;
+  }
+
+  // ---- 3. bucket-sorted in-tile order (positions are a permutation of [0, cnt))
+  {
+    const uint32_t* wh = s_wh + warp * WB * WS + (WS - 1);
+#pragma unroll
+    for (int j = 0; j < IPT; ++j) {
+      const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
+      if (FULL || pos < cnt) {
+        const uint32_t d = wh[(packed[j] >> 16) * WS] + (packed[j] & 0xFFFFu);
+        if constexpr (L::MODE == R_KEYS)
+          s_r[d] = s_k[pos];
+        else if constexpr (L::MODE == R_INDEX16)
+          reinterpret_cast<uint16_t*>(s_r)[d] = uint16_t(pos);
+        else
+          s_r[d] = (packed[j] & 0xFFFF0000u) | pos;
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- 4. scatter in bucket-sorted order: each bucket's run is one coalesced store
+#pragma unroll
+  for (int j = 0; j < IPT; ++j) {
+    const uint32_t p = uint32_t(j) * C::THREADS + tid;
+    if (FULL || p < cnt) {
+      if constexpr (L::MODE == R_KEYS) {
+        const uint32_t key = s_r[p];
+        kout[s_delta[ident(key)] + p] = key;
+      } else if constexpr (L::MODE == R_INDEX16) {
+        const uint32_t src = reinterpret_cast<const uint16_t*>(s_r)[p];
+        const uint32_t key = s_k[src];
+        const uint32_t g = s_delta[ident(key)] + p;
+        kout[g] = key;
+        vout[g] = s_v[src];
+      } else {
+        const uint32_t e = s_r[p];
+        const uint32_t src = e & 0xFFFFu;
+        const uint32_t g = s_delta[(e >> 16) & (B - 1)] + p;
+        kout[g] = s_k[src];
+        if constexpr (C::KV) vout[g] = s_v[src];
+      }
+    }
   }
 }
 
@@ -173,28 +456,23 @@ __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __r
 //  4. walk the bucket-sorted order: out[delta[b] + p] = key (value), so every
 //     bucket's run is a contiguous, coalesced store.
 template <class C, int KIND>
-__global__ void __launch_bounds__(C::THREADS) postscan_kernel(
+__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, KIND>::MIN_BLOCKS)) postscan_kernel(
     const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
     uint32_t* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
-    BucketParams bp, ScratchHeader* hdr) {
+    BucketParams bp, ScratchHeader* hdr, uint32_t prefetch_dist) {
+  using L = PostLayout<C, KIND>;
   constexpr uint32_t B = C::B;
   constexpr int LOGB = C::LOGB;
-  constexpr int IPT = C::IPT;
   constexpr uint32_t WB = C::WB;
 
   extern __shared__ __align__(128) unsigned char smem[];
-  uint32_t* s_k = reinterpret_cast<uint32_t*>(smem + C::OFF_K);
-  uint32_t* s_v = reinterpret_cast<uint32_t*>(smem + C::OFF_V);
-  uint32_t* s_r = reinterpret_cast<uint32_t*>(smem + C::OFF_R);
-  uint32_t* s_wh = reinterpret_cast<uint32_t*>(smem + C::OFF_WH);
-  uint32_t* s_delta = reinterpret_cast<uint32_t*>(smem + C::OFF_DELTA);
-  uint32_t* s_split = reinterpret_cast<uint32_t*>(smem + C::OFF_SPLIT);
-  uint32_t* s_scan = reinterpret_cast<uint32_t*>(smem + C::OFF_SCAN);
-  uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
+  uint32_t* s_k = reinterpret_cast<uint32_t*>(smem + L::OFF_K);
+  uint32_t* s_v = reinterpret_cast<uint32_t*>(smem + L::OFF_V);
+  uint32_t* s_wh = reinterpret_cast<uint32_t*>(smem + L::OFF_WH);
+  uint32_t* s_split = reinterpret_cast<uint32_t*>(smem + L::OFF_SPLIT);
+  uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
 
   const uint32_t tid = threadIdx.x;
-  const uint32_t lane = tid & 31u;
-  const uint32_t warp = tid >> 5;
   const uint32_t tile = blockIdx.x;
   const uint32_t base = tile * C::TILE;
   const uint32_t cnt = min(C::TILE, n - base);
@@ -203,21 +481,30 @@ __global__ void __launch_bounds__(C::THREADS) postscan_kernel(
   uintptr_t addr_bits = reinterpret_cast<uintptr_t>(kin);
   if constexpr (C::KV) addr_bits |= reinterpret_cast<uintptr_t>(vin);
   const uint32_t bulk = ((addr_bits & 15u) == 0) ? (cnt & ~3u) : 0u;  // elements moved by the bulk copy
+  if (tid == 0) *reinterpret_cast<uint32_t*>(smem + L::OFF_FLAG) = 0u;
   if (tid == 0 && bulk != 0) {
     mbar_init(s_bar, 1);
     fence_mbar_init();
     mbar_arrive_expect_tx(s_bar, (C::KV ? 2u : 1u) * bulk * 4u);
     bulk_copy_g2s(s_k, kin + base, bulk * 4u, s_bar);
     if constexpr (C::KV) bulk_copy_g2s(s_v, vin + base, bulk * 4u, s_bar);
+    // Blocks start roughly in tile order, so the tile `prefetch_dist` ahead
+    // (about one wave of resident blocks) starts about one tile-time from now:
+    // pull it into L2 so its bulk copy does not wait on DRAM.
+    const uint32_t ahead = tile + prefetch_dist;
+    if (prefetch_dist != 0 && ahead + 1 < num_tiles) {
+      bulk_prefetch_l2(kin + size_t(ahead) * C::TILE, C::TILE * 4u);
+      if constexpr (C::KV) bulk_prefetch_l2(vin + size_t(ahead) * C::TILE, C::TILE * 4u);
+    }
   }
   for (uint32_t i = bulk + tid; i < cnt; i += C::THREADS) {
     s_k[i] = kin[base + i];
     if constexpr (C::KV) s_v[i] = vin[base + i];
   }
   const uint32_t goff = (tid < B) ? offsets[tid * num_tiles + tile] : 0u;
-  load_splitters<KIND, LOGB>(s_split, bp);
+  prepare_identifier<KIND, LOGB>(s_split, bp);
   if constexpr (LOGB > 5) {
-    for (uint32_t i = tid; i < C::WARPS * WB; i += C::THREADS) s_wh[i] = 0u;
+    for (uint32_t i = tid; i < C::WARPS * WB * C::WS; i += C::THREADS) s_wh[i] = 0u;
   }
   __syncthreads();
   if (bulk != 0) {
@@ -231,134 +518,10 @@ __global__ void __launch_bounds__(C::THREADS) postscan_kernel(
     }
   }
 
-  // ---- 1. stable in-warp ranks
-  const Identifier<KIND, LOGB> ident{bp, s_split};
-  uint32_t packed[IPT];  // (bucket << 16) | rank among same-bucket keys of this warp
-  const uint32_t wbase = warp * (IPT * 32u);
-  const uint32_t lt = lanemask_lt();
-  if constexpr (LOGB <= 5) {
-    uint32_t xm[LOGB];
-#pragma unroll
-    for (int i = 0; i < LOGB; ++i) xm[i] = ((lane >> i) & 1u) ? 0u : ~0u;
-    uint32_t my_cnt = 0;  // keys of bucket `lane` seen so far by this warp
-#pragma unroll
-    for (int j = 0; j < IPT; ++j) {
-      const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
-      const bool valid = pos < cnt;
-      const uint32_t b = ident(s_k[pos]);
-      uint32_t m = __ballot_sync(~0u, valid);  // -> lanes holding bucket `lane`
-#pragma unroll
-      for (int i = 0; i < LOGB; ++i) m &= __ballot_sync(~0u, (b >> i) & 1u) ^ xm[i];
-      const uint32_t peers = __shfl_sync(~0u, m, b);
-      const uint32_t before = __shfl_sync(~0u, my_cnt, b);
-      packed[j] = (b << 16) | (before + __popc(peers & lt));
-      my_cnt += __popc(m);
-    }
-    if (lane < B) s_wh[warp * WB + lane] = my_cnt;
-  } else {
-    uint32_t* wh = s_wh + warp * WB;
-#pragma unroll
-    for (int j = 0; j < IPT; ++j) {
-      const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
-      const bool valid = pos < cnt;
-      const uint32_t b = ident(s_k[pos]);
-      uint32_t peers = __ballot_sync(~0u, valid);
-#pragma unroll
-      for (int i = 0; i < LOGB; ++i) {
-        const uint32_t bal = __ballot_sync(~0u, (b >> i) & 1u);
-        peers &= ((b >> i) & 1u) ? bal : ~bal;
-      }
-      const uint32_t rank = __popc(peers & lt);
-      const uint32_t before = wh[b];
-      __syncwarp();
-      if (valid && rank == 0) wh[b] = before + __popc(peers);
-      __syncwarp();
-      packed[j] = (b << 16) | (before + rank);
-    }
-  }
-  __syncthreads();
-
-  // ---- 2. tile scan
-  if (tid < B) {
-    uint32_t running = 0;
-#pragma unroll
-    for (int w = 0; w < C::WARPS; ++w) {
-      const uint32_t c = s_wh[w * WB + tid];
-      s_wh[w * WB + tid] = running;
-      running += c;
-    }
-    s_scan[tid] = running;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    constexpr uint32_t PER = (B + 31) / 32;
-    uint32_t v[PER];
-    uint32_t sum = 0;
-#pragma unroll
-    for (uint32_t k = 0; k < PER; ++k) {
-      const uint32_t idx = lane * PER + k;
-      v[k] = idx < B ? s_scan[idx] : 0u;
-      sum += v[k];
-    }
-    uint32_t incl = sum;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t t = __shfl_up_sync(~0u, incl, d);
-      if (lane >= uint32_t(d)) incl += t;
-    }
-    uint32_t excl = incl - sum;
-#pragma unroll
-    for (uint32_t k = 0; k < PER; ++k) {
-      const uint32_t idx = lane * PER + k;
-      if (idx < B) s_scan[idx] = excl;
-      excl += v[k];
-    }
-  }
-  __syncthreads();
-  if (tid < B) {
-    const uint32_t start = s_scan[tid];
-    s_delta[tid] = goff - start;
-#pragma unroll
-    for (int w = 0; w < C::WARPS; ++w) s_wh[w * WB + tid] += start;
-  }
-  __syncthreads();
-
-  // ---- 3. bucket-sorted in-tile order
-  bool bad = false;
-  {
-    const uint32_t* wh = s_wh + warp * WB;
-#pragma unroll
-    for (int j = 0; j < IPT; ++j) {
-      const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
-      if (pos < cnt) {
-        const uint32_t b = packed[j] >> 16;
-        const uint32_t d = wh[b] + (packed[j] & 0xFFFFu);
-        if (d < cnt)
-          s_r[d] = (b << 16) | pos;
-        else
-          bad = true;
-      }
-    }
-  }
-  __syncthreads();
-
-  // ---- 4. scatter (positions are checked: a corrupt offset is reported, never written)
-#pragma unroll
-  for (int j = 0; j < IPT; ++j) {
-    const uint32_t p = uint32_t(j) * C::THREADS + tid;
-    if (p < cnt) {
-      const uint32_t e = s_r[p];
-      const uint32_t src = e & 0xFFFFu;
-      const uint32_t g = s_delta[(e >> 16) & (B - 1)] + p;
-      if (g < n && src < cnt) {
-        kout[g] = s_k[src];
-        if constexpr (C::KV) vout[g] = s_v[src];
-      } else {
-        bad = true;
-      }
-    }
-  }
-  if (bad) record_error(hdr, DEV_ERR_BAD_OFFSET);
+  if (cnt == C::TILE)
+    postscan_tile<C, KIND, true>(kout, vout, n, cnt, goff, bp, hdr, smem);
+  else
+    postscan_tile<C, KIND, false>(kout, vout, n, cnt, goff, bp, hdr, smem);
 }
 
 }  // namespace gms

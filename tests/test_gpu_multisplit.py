@@ -190,3 +190,32 @@ def test_errors_are_reported(gms_lib):
         gms.multisplit_key_only(dk, ok, 100000, ctx, gms.delta_bucket())
     with pytest.raises(gms.GmsError):  # in place is not supported
         gms.multisplit_key_only(dk, dk, 1000, ctx, gms.delta_bucket())
+
+
+@pytest.mark.parametrize("B", [4, 32, 256])
+@pytest.mark.parametrize("with_values", [False, True], ids=["keys", "pairs"])
+def test_range_adversarial_splitters(gms_lib, oracle_mod, B, with_values):
+    """Splitters packed into one narrow key range, with duplicates and a first
+    splitter above zero (keys below it wrap to bucket B-1), and keys aimed at
+    the splitters themselves and their neighbours."""
+    o = oracle_mod
+    rng = np.random.default_rng(B)
+    base = np.uint32(0x12345600)
+    spl = np.sort((base + rng.integers(0, 3 * B, B)).astype(np.uint32))
+    spl[B // 2] = spl[B // 2 - 1]  # a duplicate splitter
+    n = 70001
+    keys = np.concatenate([spl, spl - np.uint32(1), spl + np.uint32(1),
+                           rng.integers(0, 2**32, n - 3 * B, dtype=np.uint64).astype(np.uint32)])
+    rng.shuffle(keys)
+    d_spl = datagen.from_u32(spl, "cuda")
+    vals = np.arange(n, dtype=np.uint32) if with_values else None
+    gk, gv, offs, err = run_multisplit(keys, B, gms.range_bucket(d_spl), vals)
+    rk, rv, roffs = o.multisplit(keys, o.Desc(o.RANGE, B, splitters=spl), vals)
+    assert err == 0
+    np.testing.assert_array_equal(gk, rk)
+    if with_values:
+        np.testing.assert_array_equal(gv, rv)
+    assert offs == [int(x) for x in roffs]
+    hist = torch.zeros(B, dtype=torch.int32, device="cuda")
+    gms.histogram_range(to_dev(keys), n, hist, B, d_spl)
+    np.testing.assert_array_equal(hist.cpu().numpy(), o.histogram(keys, o.Desc(o.RANGE, B, splitters=spl)))
