@@ -32,6 +32,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -53,6 +55,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline time budget")
+    p.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
+    p.add_argument("--only-batched", action="store_true", help="print only the batched-form summary")
     return p.parse_args()
 
 
@@ -174,6 +178,85 @@ def ncu_traffic(kernel: str, n: int):
         return None
 
 
+def run_batched(dev, reps: int = 3):
+    """Batched form (4096 segments, log-uniform sizes in [1024, 4194304], seed 7,
+    B in {2, 8, 32, 256}, delta or range identifier, key-value) against the plain
+    per-call loop over the same segments; returns a summary dict."""
+    import torch
+
+    import gpumultisplit_gb300 as gms
+    from gpumultisplit_gb300 import datagen
+
+    sizes, buckets, kinds = datagen.batched_spec()
+    # segment starts padded to 32 elements so every segment is 16-byte aligned
+    starts = np.concatenate([[0], np.cumsum((sizes + 31) // 32 * 32)[:-1]]).astype(np.int64)
+    total_alloc = int(starts[-1] + (sizes[-1] + 31) // 32 * 32)
+    total = int(sizes.sum())
+    keys = datagen.uniform_u32(total_alloc, 11, device=dev)
+    vals = datagen.index_values(total_alloc, dev)
+    kout, vout = torch.zeros_like(keys), torch.zeros_like(vals)
+    kref, vref = torch.zeros_like(keys), torch.zeros_like(vals)
+    segs, plain = [], []
+    for i, (n, B, kind) in enumerate(zip(sizes.tolist(), buckets.tolist(), kinds)):
+        o = int(starts[i])
+        ident = gms.delta_bucket() if kind == "delta" else gms.range_bucket(datagen.range_splitters(B, 1000 + i, dev))
+        segs.append(gms.Segment(keys[o:o + n], kout[o:o + n], n, B, ident, vals[o:o + n], vout[o:o + n]))
+        plain.append((keys[o:o + n], vals[o:o + n], kref[o:o + n], vref[o:o + n], n, B, ident))
+    ctxs = {}
+    for B in sorted(set(buckets.tolist())):
+        ctx = gms.multisplit_context(B)
+        gms.multisplit_allocate_key_value(int(sizes[buckets == B].max()), ctx)
+        ctxs[B] = ctx
+
+    def plain_loop():
+        for ki, vi, ko, vo, n, B, ident in plain:
+            gms.multisplit_key_value(ki, vi, ko, vo, n, ctxs[B], ident)
+
+    plan = gms.BatchedMultisplit(segs)
+
+    def timed(fn, count):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record()
+        for _ in range(count):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / count, (time.perf_counter() - t0) * 1e3 / count
+
+    plain_loop()
+    plan.run(use_graph=True)
+    plan.run(use_graph=False)
+    torch.cuda.synchronize()
+    plain_ms, plain_wall = timed(plain_loop, reps)
+    graph_ms, _ = timed(lambda: plan.run(use_graph=True), max(reps, 5))
+    nograph_ms, _ = timed(lambda: plan.run(use_graph=False), max(reps, 5))
+    identical = bool(torch.equal(kout, kref) and torch.equal(vout, vref))
+    peak, _ = hbm_peak()
+    res = {
+        "workload": f"{len(sizes)} key-value segments, sizes log-uniform in [1024, 4194304] (seed 7), "
+                    f"B in {{2,8,32,256}}, delta or range identifier; {total} pairs",
+        "pairs": total,
+        "batched_graph_ms": graph_ms,
+        "batched_graph_gkeys": total / (graph_ms * 1e-3) / 1e9,
+        "batched_nograph_ms": nograph_ms,
+        "plain_per_call_ms": plain_ms,
+        "plain_per_call_gkeys": total / (plain_ms * 1e-3) / 1e9,
+        "plain_host_wall_ms": plain_wall,
+        "speedup_vs_plain": plain_ms / graph_ms,
+        "batched_hbm_frac": 20.0 * total / (graph_ms * 1e-3) / 1e9 / peak,
+        "launches_per_run": plan.launches,
+        "plain_launches_per_run": 3 * len(sizes),
+        "identical_to_plain": identical,
+        "device_error": plan.device_error(),
+    }
+    plan.close()
+    del keys, vals, kout, vout, kref, vref, segs, plain
+    torch.cuda.empty_cache()
+    return res
+
+
 def cpu_baseline(a, keys_dev, vals_dev, seconds):
     """Times the oracle's multi-threaded restatement on a bounded sample."""
     import oracle
@@ -245,6 +328,12 @@ def run_ours(a):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if a.only_batched:
+        from gpumultisplit_gb300 import build as gbuild
+
+        gbuild.build()
+        print(json.dumps(run_batched(dev)), flush=True)
+        return
     if world > 1:
         import torch.distributed as dist
 
@@ -371,7 +460,12 @@ def run_ours(a):
         "stages_ms": {"prescan": statistics.mean(pre), "scan": statistics.mean(scan), "postscan": post_ms},
         "clocks": clocks, "gpu_launches": 3 * a.steps, "e2e": e2e,
     }
+    if not a.no_batched:
+        del keys, vals, kout, vout
+        torch.cuda.empty_cache()
+        line["batched"] = run_batched(dev)
     if rank == 0 and not a.no_cpu_baseline:
+        keys, vals, _ = make_inputs(a, dev)
         line["cpu_baseline"] = cpu_baseline(a, keys, vals, a.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -38,3 +38,4 @@ from .api import (  # noqa: F401
     test_bucket,
 )
 from ._lib import GmsError, load  # noqa: F401
+from .batched import BatchedMultisplit, Segment  # noqa: F401

@@ -79,6 +79,11 @@ _PROTOS = {
     "gms_compaction_scratch_bytes": [_U32, _I32, _PSZ],
     "gms_compaction_key_only": [_P, _P, _U32, _PDESC, _P, _SZ, _PU32, _P],
     "gms_compaction_key_value": [_P, _P, _P, _P, _U32, _PDESC, _P, _SZ, _PU32, _P],
+    "gms_batch_create": [_P, _U32, _P],
+    "gms_batch_scratch_bytes": [_P, _PSZ],
+    "gms_batch_run": [_P, _P, _SZ, _I32, _P],
+    "gms_batch_launch_count": [_P, _PU32],
+    "gms_batch_destroy": [_P],
     "gms_histogram": [_P, _U32, _PDESC, _P, _P],
     "gms_histogram_even": [_P, _U32, _P, _U32, _U32, _U32, ctypes.c_float, _P],
     "gms_histogram_range": [_P, _U32, _P, _U32, _P, _P],

@@ -1,0 +1,279 @@
+// Host side of the batched multisplit: plan construction (segment classes,
+// tile maps, count-matrix layout, scan groups), table upload, the launch
+// sequence and its capture into a CUDA graph.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "../../include/gpumultisplit.h"
+#include "batch_kernels.cuh"
+#include "ms_host.h"
+
+namespace gms {
+namespace {
+
+struct BatchClass {
+  int kind = 0;
+  int logb = 1;
+  bool kv = false;
+  std::vector<uint2> tiles;  // (segment, tile)
+  size_t map_off = 0;        // byte offset of this class's map in scratch
+};
+
+// A run of consecutive segments whose n sum stays below 2^32, scanned on its own.
+struct ScanGroup {
+  uint32_t matrix_first = 0;  // first matrix entry
+  uint32_t m = 0;             // entries
+};
+
+}  // namespace
+}  // namespace gms
+
+struct gms_batch_s {
+  std::vector<gms::SegDesc> segs;
+  std::vector<gms::BatchClass> classes;
+  std::vector<gms::ScanGroup> groups;
+  size_t off_segs = 0, off_maps = 0, off_matrix = 0, off_status = 0, bytes = 0;
+  uint32_t max_chunks = 0;
+  // Bound scratch (tables uploaded) and the captured graph for it.
+  std::mutex mu;
+  void* bound = nullptr;
+  cudaStream_t capture_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  void* graph_scratch = nullptr;
+};
+
+namespace gms {
+namespace {
+
+gms_status to_status(cudaError_t e) {
+  if (e == cudaSuccess) return GMS_SUCCESS;
+  note_cuda_error(e);
+  return GMS_ERROR_CUDA;
+}
+
+bool log2_buckets(uint32_t b, int* logb) {
+  if (b < 2 || b > 256 || (b & (b - 1)) != 0) return false;
+  int l = 0;
+  while ((1u << l) < b) ++l;
+  *logb = l;
+  return true;
+}
+
+cudaError_t dispatch_class(int kind, const BatchClassLaunch& c, int stage) {
+  switch (kind) {
+    case KIND_DELTA: return run_batch_class<KIND_DELTA>(c, stage);
+    case KIND_DIV: return run_batch_class<KIND_DIV>(c, stage);
+    case KIND_BITS: return run_batch_class<KIND_BITS>(c, stage);
+    case KIND_RANGE: return run_batch_class<KIND_RANGE>(c, stage);
+    case KIND_MASK: return run_batch_class<KIND_MASK>(c, stage);
+    case KIND_EVEN_FLOAT: return run_batch_class<KIND_EVEN_FLOAT>(c, stage);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// The launch sequence of one run: reset the error word, prescan every class,
+// scan every group (ticket and status words reset first), postscan every class.
+cudaError_t launch_all(gms_batch_s* b, unsigned char* scratch, cudaStream_t s) {
+  auto* hdr = reinterpret_cast<ScratchHeader*>(scratch);
+  auto* matrix = reinterpret_cast<uint32_t*>(scratch + b->off_matrix);
+  auto* status = reinterpret_cast<uint64_t*>(scratch + b->off_status);
+  cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(ScratchHeader), s);
+  if (e != cudaSuccess) return e;
+  BatchClassLaunch L;
+  L.segs = reinterpret_cast<const SegDesc*>(scratch + b->off_segs);
+  L.matrix = matrix;
+  L.hdr = hdr;
+  L.stream = s;
+  for (int stage : {int(STAGE_PRESCAN), int(STAGE_POSTSCAN)}) {
+    if (stage == STAGE_POSTSCAN) {
+      for (const ScanGroup& g : b->groups) {
+        e = cudaMemsetAsync(&hdr->ticket, 0, sizeof(uint32_t), s);
+        if (e == cudaSuccess)
+          e = cudaMemsetAsync(status, 0, size_t((g.m + kScanChunk - 1) / kScanChunk) * sizeof(uint64_t), s);
+        if (e == cudaSuccess) e = run_scan(matrix + g.matrix_first, g.m, status, hdr, s);
+        if (e != cudaSuccess) return e;
+      }
+    }
+    for (const BatchClass& c : b->classes) {
+      L.logb = c.logb;
+      L.kv = c.kv;
+      L.tile_map = reinterpret_cast<const uint2*>(scratch + c.map_off);
+      L.class_tiles = uint32_t(c.tiles.size());
+      e = dispatch_class(c.kind, L, stage);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace gms
+
+using namespace gms;
+
+extern "C" {
+
+gms_status gms_batch_create(const gms_segment* segments, uint32_t count, gms_batch_t* batch) {
+  if (batch == nullptr || (segments == nullptr && count > 0)) return GMS_ERROR_INVALID_VALUE;
+  auto* b = new gms_batch_s();
+  std::map<std::tuple<int, int, bool>, size_t> class_index;
+  uint64_t matrix_total = 0, group_n = 0;
+  ScanGroup group;
+  for (uint32_t i = 0; i < count; ++i) {
+    const gms_segment& sg = segments[i];
+    int logb = 0;
+    if (!log2_buckets(sg.desc.num_buckets, &logb)) {
+      delete b;
+      return GMS_ERROR_UNSUPPORTED_BUCKETS;
+    }
+    const bool kv = sg.d_value_in != nullptr;
+    const int kind = sg.desc.kind;
+    const bool bad_desc = kind < 0 || kind >= NUM_KINDS || (kind == KIND_DIV && sg.desc.param == 0) ||
+                          (kind == KIND_RANGE && sg.desc.d_splitters == nullptr);
+    const bool bad_ptrs = sg.n > 0 && (sg.d_key_in == nullptr || sg.d_key_out == nullptr ||
+                                       (kv && sg.d_value_out == nullptr) || (!kv && sg.d_value_out != nullptr));
+    if (bad_desc || bad_ptrs) {
+      delete b;
+      return GMS_ERROR_INVALID_VALUE;
+    }
+    SegDesc d{};
+    d.kin = sg.d_key_in;
+    d.vin = sg.d_value_in;
+    d.kout = sg.d_key_out;
+    d.vout = sg.d_value_out;
+    d.n = sg.n;
+    d.bp.shift = sg.desc.shift;
+    d.bp.param = sg.desc.param;
+    d.bp.lower = sg.desc.lower;
+    d.bp.inverse_delta = sg.desc.inverse_delta;
+    d.bp.splitters = sg.desc.d_splitters;
+    const uint32_t tile = tile_keys(logb, kv);
+    d.num_tiles = uint32_t((uint64_t(sg.n) + tile - 1) / tile);
+    const uint64_t entries = uint64_t(1u << logb) * d.num_tiles;
+    // Start a new scan group when this segment would push the group's keys past 2^32 - 1.
+    if (group_n + sg.n > 0xFFFFFFFFull) {
+      group.m = uint32_t(matrix_total - group.matrix_first);
+      b->groups.push_back(group);
+      group.matrix_first = uint32_t(matrix_total);
+      group_n = 0;
+    }
+    d.base = uint32_t(group_n);
+    d.matrix_off = uint32_t(matrix_total);
+    group_n += sg.n;
+    matrix_total += entries;
+    if (matrix_total > 0xFFFFFFFFull) {
+      delete b;
+      return GMS_ERROR_NOT_SUPPORTED;
+    }
+    b->segs.push_back(d);
+    if (d.num_tiles == 0) continue;
+    const auto key = std::make_tuple(kind, logb, kv);
+    auto it = class_index.find(key);
+    if (it == class_index.end()) {
+      it = class_index.emplace(key, b->classes.size()).first;
+      BatchClass c;
+      c.kind = kind;
+      c.logb = logb;
+      c.kv = kv;
+      b->classes.push_back(c);
+    }
+    auto& tiles = b->classes[it->second].tiles;
+    for (uint32_t t = 0; t < d.num_tiles; ++t) tiles.push_back(make_uint2(i, t));
+  }
+  group.m = uint32_t(matrix_total - group.matrix_first);
+  if (group.m > 0) b->groups.push_back(group);
+  for (const ScanGroup& g : b->groups)
+    b->max_chunks = std::max(b->max_chunks, (g.m + kScanChunk - 1) / kScanChunk);
+
+  size_t off = sizeof(ScratchHeader);
+  b->off_segs = off;
+  off = align_up(off + b->segs.size() * sizeof(SegDesc), 256);
+  b->off_maps = off;
+  for (BatchClass& c : b->classes) {
+    c.map_off = off;
+    off = align_up(off + c.tiles.size() * sizeof(uint2), 256);
+  }
+  b->off_matrix = off;
+  off = align_up(off + size_t(matrix_total) * 4, 256);
+  b->off_status = off;
+  b->bytes = align_up(off + size_t(b->max_chunks) * 8, 256);
+  *batch = b;
+  return GMS_SUCCESS;
+}
+
+gms_status gms_batch_scratch_bytes(gms_batch_t batch, size_t* bytes) {
+  if (batch == nullptr || bytes == nullptr) return GMS_ERROR_INVALID_VALUE;
+  *bytes = batch->bytes;
+  return GMS_SUCCESS;
+}
+
+gms_status gms_batch_launch_count(gms_batch_t batch, uint32_t* launches) {
+  if (batch == nullptr || launches == nullptr) return GMS_ERROR_INVALID_VALUE;
+  uint32_t n = 0;
+  for (const BatchClass& c : batch->classes) n += c.tiles.empty() ? 0u : 2u;
+  for (const ScanGroup& g : batch->groups) n += g.m > 0 ? 1u : 0u;
+  *launches = n;
+  return GMS_SUCCESS;
+}
+
+gms_status gms_batch_run(gms_batch_t b, void* d_scratch, size_t scratch_bytes, int use_graph,
+                         gms_stream_t stream) {
+  if (b == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (b->classes.empty()) return GMS_SUCCESS;
+  if (d_scratch == nullptr || (reinterpret_cast<uintptr_t>(d_scratch) & 255u) != 0)
+    return GMS_ERROR_INVALID_VALUE;
+  if (scratch_bytes < b->bytes) return GMS_ERROR_SCRATCH_TOO_SMALL;
+  std::lock_guard<std::mutex> lock(b->mu);
+  auto* scratch = static_cast<unsigned char*>(d_scratch);
+  cudaError_t e = cudaSuccess;
+  if (b->bound != d_scratch) {
+    e = cudaMemcpyAsync(scratch + b->off_segs, b->segs.data(), b->segs.size() * sizeof(SegDesc),
+                        cudaMemcpyHostToDevice, stream);
+    for (size_t i = 0; e == cudaSuccess && i < b->classes.size(); ++i) {
+      const BatchClass& c = b->classes[i];
+      e = cudaMemcpyAsync(scratch + c.map_off, c.tiles.data(), c.tiles.size() * sizeof(uint2),
+                          cudaMemcpyHostToDevice, stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return to_status(e);
+    b->bound = d_scratch;
+  }
+  if (!use_graph) return to_status(launch_all(b, scratch, stream));
+
+  if (b->exec == nullptr || b->graph_scratch != d_scratch) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    if (b->capture_stream == nullptr) {
+      e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
+      if (e != cudaSuccess) return to_status(e);
+    }
+    e = cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return to_status(e);
+    const cudaError_t le = launch_all(b, scratch, b->capture_stream);
+    e = cudaStreamEndCapture(b->capture_stream, &b->graph);
+    if (le != cudaSuccess) return to_status(le);
+    if (e != cudaSuccess) return to_status(e);
+    e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (e != cudaSuccess) return to_status(e);
+    b->graph_scratch = d_scratch;
+  }
+  return to_status(cudaGraphLaunch(b->exec, stream));
+}
+
+gms_status gms_batch_destroy(gms_batch_t b) {
+  if (b == nullptr) return GMS_SUCCESS;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+  delete b;
+  return GMS_SUCCESS;
+}
+
+}  // extern "C"

@@ -78,6 +78,25 @@ cudaError_t run_histogram(const uint32_t* keys, uint32_t n, int logb, const Buck
 
 cudaError_t run_scan(uint32_t* data, uint32_t m, uint64_t* status, ScratchHeader* hdr, cudaStream_t stream);
 
+struct SegDesc;
+
+// One class of a batched multisplit (same kind, log2 B and key/value shape).
+struct BatchClassLaunch {
+  int logb = 1;
+  bool kv = false;
+  const SegDesc* segs = nullptr;    // device
+  const uint2* tile_map = nullptr;  // device, class_tiles entries of (segment, tile)
+  uint32_t class_tiles = 0;
+  uint32_t* matrix = nullptr;       // device, the batch count matrix
+  ScratchHeader* hdr = nullptr;
+  cudaStream_t stream = nullptr;
+};
+
+// Launches the prescan (STAGE_PRESCAN) or postscan (STAGE_POSTSCAN) of one
+// batch class.  Defined per identifier kind in inst_*.cu.
+template <int KIND>
+cudaError_t run_batch_class(const BatchClassLaunch& c, int stage);
+
 int device_sm_count();
 
 // Records a CUDA error for gms_last_cuda_error() (calling thread).

@@ -444,7 +444,22 @@ __device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint3
 }
 
 // -------------------------------------------------------------- postscan
-// One CTA per tile.
+// One tile of one multisplit, as the postscan sees it.
+struct TileJob {
+  const uint32_t* kin;
+  const uint32_t* vin;
+  uint32_t* kout;
+  uint32_t* vout;
+  uint32_t n;                // keys of this multisplit
+  uint32_t num_tiles;        // its tiles
+  uint32_t tile;             // this tile
+  const uint32_t* offsets;   // its scanned count matrix, bucket-major
+  uint32_t bias;             // subtracted from the scanned offsets (start of this multisplit in a shared scan)
+  uint32_t prefetch_tile;    // a later tile of the same arrays to pull into L2 (>= num_tiles: none)
+  BucketParams bp;
+};
+
+// Postscan of one tile, run by a whole block:
 //  0. bulk-copy the tile's keys (and values) into shared memory, prefetch the
 //     tile's B global offsets;
 //  1. per warp, stable rank of every key among same-bucket keys earlier in the
@@ -452,20 +467,15 @@ __device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint3
 //     key w*IPT*32 + j*32 + l);
 //  2. tile scan: per-warp bucket offsets and the per-bucket shift
 //     delta[b] = global_offset(b, tile) - tile_start(b);
-//  3. write, at each key's bucket-sorted in-tile position, its source index;
+//  3. write, at each key's bucket-sorted in-tile position, its key or source index;
 //  4. walk the bucket-sorted order: out[delta[b] + p] = key (value), so every
 //     bucket's run is a contiguous, coalesced store.
 template <class C, int KIND>
-__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, KIND>::MIN_BLOCKS)) postscan_kernel(
-    const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
-    uint32_t* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
-    BucketParams bp, ScratchHeader* hdr, uint32_t prefetch_dist) {
+__device__ __forceinline__ void postscan_job(const TileJob& job, ScratchHeader* hdr, unsigned char* smem) {
   using L = PostLayout<C, KIND>;
   constexpr uint32_t B = C::B;
   constexpr int LOGB = C::LOGB;
   constexpr uint32_t WB = C::WB;
-
-  extern __shared__ __align__(128) unsigned char smem[];
   uint32_t* s_k = reinterpret_cast<uint32_t*>(smem + L::OFF_K);
   uint32_t* s_v = reinterpret_cast<uint32_t*>(smem + L::OFF_V);
   uint32_t* s_wh = reinterpret_cast<uint32_t*>(smem + L::OFF_WH);
@@ -473,9 +483,10 @@ __global__ void __launch_bounds__(C::THREADS, (PostLayout<C, KIND>::MIN_BLOCKS))
   uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
 
   const uint32_t tid = threadIdx.x;
-  const uint32_t tile = blockIdx.x;
-  const uint32_t base = tile * C::TILE;
-  const uint32_t cnt = min(C::TILE, n - base);
+  const uint32_t base = job.tile * C::TILE;
+  const uint32_t cnt = min(C::TILE, job.n - base);
+  const uint32_t* kin = job.kin;
+  const uint32_t* vin = job.vin;
 
   // ---- 0. stage the tile
   uintptr_t addr_bits = reinterpret_cast<uintptr_t>(kin);
@@ -488,21 +499,19 @@ __global__ void __launch_bounds__(C::THREADS, (PostLayout<C, KIND>::MIN_BLOCKS))
     mbar_arrive_expect_tx(s_bar, (C::KV ? 2u : 1u) * bulk * 4u);
     bulk_copy_g2s(s_k, kin + base, bulk * 4u, s_bar);
     if constexpr (C::KV) bulk_copy_g2s(s_v, vin + base, bulk * 4u, s_bar);
-    // Blocks start roughly in tile order, so the tile `prefetch_dist` ahead
-    // (about one wave of resident blocks) starts about one tile-time from now:
-    // pull it into L2 so its bulk copy does not wait on DRAM.
-    const uint32_t ahead = tile + prefetch_dist;
-    if (prefetch_dist != 0 && ahead + 1 < num_tiles) {
-      bulk_prefetch_l2(kin + size_t(ahead) * C::TILE, C::TILE * 4u);
-      if constexpr (C::KV) bulk_prefetch_l2(vin + size_t(ahead) * C::TILE, C::TILE * 4u);
+    // Pull a tile that starts about one wave of blocks later into L2, so its
+    // bulk copy does not wait on DRAM (only full tiles: never past the arrays).
+    if (job.prefetch_tile < job.num_tiles - 1u) {
+      bulk_prefetch_l2(kin + size_t(job.prefetch_tile) * C::TILE, C::TILE * 4u);
+      if constexpr (C::KV) bulk_prefetch_l2(vin + size_t(job.prefetch_tile) * C::TILE, C::TILE * 4u);
     }
   }
   for (uint32_t i = bulk + tid; i < cnt; i += C::THREADS) {
     s_k[i] = kin[base + i];
     if constexpr (C::KV) s_v[i] = vin[base + i];
   }
-  const uint32_t goff = (tid < B) ? offsets[tid * num_tiles + tile] : 0u;
-  prepare_identifier<KIND, LOGB>(s_split, bp);
+  const uint32_t goff = (tid < B) ? job.offsets[tid * job.num_tiles + job.tile] - job.bias : 0u;
+  prepare_identifier<KIND, LOGB>(s_split, job.bp);
   if constexpr (LOGB > 5) {
     for (uint32_t i = tid; i < C::WARPS * WB * C::WS; i += C::THREADS) s_wh[i] = 0u;
   }
@@ -512,16 +521,38 @@ __global__ void __launch_bounds__(C::THREADS, (PostLayout<C, KIND>::MIN_BLOCKS))
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
         record_error(hdr, DEV_ERR_BULK_COPY_TIMEOUT);
-        mbar_wait_bounded(s_bar, 0);  // let a late copy land before the CTA exits
+        mbar_wait_bounded(s_bar, 0);  // let a late copy land before the block moves on
       }
       return;
     }
   }
 
   if (cnt == C::TILE)
-    postscan_tile<C, KIND, true>(kout, vout, n, cnt, goff, bp, hdr, smem);
+    postscan_tile<C, KIND, true>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
   else
-    postscan_tile<C, KIND, false>(kout, vout, n, cnt, goff, bp, hdr, smem);
+    postscan_tile<C, KIND, false>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
+}
+
+// Plain postscan: one block per tile of one multisplit.
+template <class C, int KIND>
+__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, KIND>::MIN_BLOCKS)) postscan_kernel(
+    const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
+    uint32_t* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
+    BucketParams bp, ScratchHeader* hdr, uint32_t prefetch_dist) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  TileJob job;
+  job.kin = kin;
+  job.vin = vin;
+  job.kout = kout;
+  job.vout = vout;
+  job.n = n;
+  job.num_tiles = num_tiles;
+  job.tile = blockIdx.x;
+  job.offsets = offsets;
+  job.bias = 0u;
+  job.prefetch_tile = prefetch_dist != 0 ? blockIdx.x + prefetch_dist : ~0u;
+  job.bp = bp;
+  postscan_job<C, KIND>(job, hdr, smem);
 }
 
 }  // namespace gms

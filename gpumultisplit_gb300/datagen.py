@@ -121,3 +121,15 @@ def as_u32(t: torch.Tensor) -> np.ndarray:
 
 def from_u32(a: np.ndarray, device="cpu") -> torch.Tensor:
     return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint32).view(np.int32)).to(device)
+
+
+def batched_spec(count: int = 4096, seed: int = 7, buckets=(2, 8, 32, 256), kinds=("delta", "range"),
+                 lo: int = 1024, hi: int = 4194304):
+    """Segments of the batched workload: log-uniform sizes in [lo, hi] (seed), and
+    per segment a bucket count and identifier kind drawn from `buckets` / `kinds`
+    (seed + 1).  Returns (sizes, bucket counts, kinds) as numpy arrays / list."""
+    sizes = segment_sizes(count, seed, lo, hi)
+    u = uniform_unit(2 * count, seed + 1).numpy()
+    b = np.array(buckets)[np.minimum((u[:count] * len(buckets)).astype(np.int64), len(buckets) - 1)]
+    k = [kinds[min(int(x * len(kinds)), len(kinds) - 1)] for x in u[count:]]
+    return sizes, b, k

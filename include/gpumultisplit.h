@@ -177,6 +177,39 @@ gms_status gms_compaction_key_value(const uint32_t* d_key_in, const uint32_t* d_
                                     void* d_scratch, size_t scratch_bytes, uint32_t* h_num_bucket0,
                                     gms_stream_t stream);
 
+/* -------------------------------------------------------------- batched */
+/* Many independent multisplits of uneven sizes and bucket counts ("segments")
+ * run as one plan: per stage one launch per segment class (identifier kind,
+ * bucket count, key/value shape) over a device-side tile map, and one scan over
+ * all segments' count matrices laid end to end; optionally captured once into a
+ * CUDA graph and replayed.  No reference counterpart (the reference runs one
+ * multisplit per call, src/api/multisplit.cuh:81-313); each segment's output
+ * equals gms_multisplit_key_value / _key_only on that segment alone. */
+typedef struct gms_segment {
+  const uint32_t* d_key_in;
+  const uint32_t* d_value_in; /* null: key-only segment */
+  uint32_t* d_key_out;
+  uint32_t* d_value_out;      /* null iff d_value_in is null */
+  uint32_t n;
+  gms_bucket_desc desc;
+} gms_segment;
+
+typedef struct gms_batch_s* gms_batch_t;
+
+/* Builds a plan for `count` segments (host work only; the segment array is copied). */
+gms_status gms_batch_create(const gms_segment* segments, uint32_t count, gms_batch_t* batch);
+/* Scratch the plan needs: tables, count matrix, scan state. */
+gms_status gms_batch_scratch_bytes(gms_batch_t batch, size_t* bytes);
+/* Runs every segment's multisplit on `stream`.  The first run with a given
+ * scratch buffer uploads the plan's tables there (and synchronises); with
+ * use_graph != 0 the launch sequence is captured once into a CUDA graph (per
+ * scratch buffer) and replayed with one graph launch per call. */
+gms_status gms_batch_run(gms_batch_t batch, void* d_scratch, size_t scratch_bytes, int use_graph,
+                         gms_stream_t stream);
+/* Number of kernel launches one run issues (inside the graph when use_graph != 0). */
+gms_status gms_batch_launch_count(gms_batch_t batch, uint32_t* launches);
+gms_status gms_batch_destroy(gms_batch_t batch);
+
 /* ------------------------------------------------------------ histogram */
 /* Adds the per-bucket counts of d_key_in[0..n) into d_hist[0..B) (the caller
  * zeroes it first, as with the reference's atomicAdd kernels).  Generalises
