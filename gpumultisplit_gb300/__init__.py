@@ -39,3 +39,4 @@ from .api import (  # noqa: F401
 )
 from ._lib import GmsError, load  # noqa: F401
 from .batched import BatchedMultisplit, Segment  # noqa: F401
+from .serving import Result, Server  # noqa: F401

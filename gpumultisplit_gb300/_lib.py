@@ -84,11 +84,22 @@ _PROTOS = {
     "gms_batch_run": [_P, _P, _SZ, _I32, _P],
     "gms_batch_launch_count": [_P, _PU32],
     "gms_batch_destroy": [_P],
+    "gms_server_create": [_P, _SZ, _P],
+    "gms_server_submit": [_P, _P, _P],
+    "gms_server_poll": [_P, ctypes.c_uint64, _P],
+    "gms_server_wait": [_P, ctypes.c_uint64, _P],
+    "gms_server_take_completed": [_P, _P, _U32, _PU32],
+    "gms_server_release": [_P, ctypes.c_uint64],
+    "gms_server_drain": [_P],
+    "gms_server_get_stats": [_P, _P],
+    "gms_server_clock": [_P],
+    "gms_server_destroy": [_P],
     "gms_histogram": [_P, _U32, _PDESC, _P, _P],
     "gms_histogram_even": [_P, _U32, _P, _U32, _U32, _U32, ctypes.c_float, _P],
     "gms_histogram_range": [_P, _U32, _P, _U32, _P, _P],
 }
-_RESTYPES = {"gms_version": ctypes.c_int, "gms_status_string": ctypes.c_char_p, "gms_last_cuda_error": ctypes.c_int}
+_RESTYPES = {"gms_version": ctypes.c_int, "gms_status_string": ctypes.c_char_p, "gms_last_cuda_error": ctypes.c_int,
+             "gms_server_clock": ctypes.c_double}
 
 # Symbols declared in include/*.h (checked by the CPU test suite).
 EXPORTED = tuple(_PROTOS)

@@ -267,6 +267,41 @@ gms_status gms_batch_run(gms_batch_t b, void* d_scratch, size_t scratch_bytes, i
   return to_status(cudaGraphLaunch(b->exec, stream));
 }
 
+}  // extern "C"
+
+namespace gms {
+
+size_t batch_table_bytes(gms_batch_t b) { return b->off_matrix - b->off_segs; }
+
+gms_status batch_run_async(gms_batch_t b, void* d_scratch, size_t scratch_bytes, void* h_pinned,
+                           size_t pinned_bytes, cudaStream_t stream) {
+  if (b == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (b->classes.empty()) return GMS_SUCCESS;
+  const size_t table = batch_table_bytes(b);
+  if (d_scratch == nullptr || scratch_bytes < b->bytes || h_pinned == nullptr || pinned_bytes < table)
+    return GMS_ERROR_INVALID_VALUE;
+  // Stage the segment table and tile maps in pinned memory at their scratch offsets, then one copy.
+  auto* staging = static_cast<unsigned char*>(h_pinned);
+  std::memcpy(staging, b->segs.data(), b->segs.size() * sizeof(SegDesc));
+  for (const BatchClass& c : b->classes)
+    std::memcpy(staging + (c.map_off - b->off_segs), c.tiles.data(), c.tiles.size() * sizeof(uint2));
+  auto* scratch = static_cast<unsigned char*>(d_scratch);
+  cudaError_t e = cudaMemcpyAsync(scratch + b->off_segs, staging, table, cudaMemcpyHostToDevice, stream);
+  if (e == cudaSuccess) e = launch_all(b, scratch, stream);
+  return to_status(e);
+}
+
+uint32_t batch_matrix_value_offset(gms_batch_t b, uint32_t segment, uint32_t bucket, uint32_t tile,
+                                   uint32_t* base) {
+  const SegDesc& d = b->segs[segment];
+  *base = d.base;
+  return uint32_t(b->off_matrix / 4) + d.matrix_off + bucket * d.num_tiles + tile;
+}
+
+}  // namespace gms
+
+extern "C" {
+
 gms_status gms_batch_destroy(gms_batch_t b) {
   if (b == nullptr) return GMS_SUCCESS;
   if (b->exec) cudaGraphExecDestroy(b->exec);

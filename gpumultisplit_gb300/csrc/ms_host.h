@@ -7,6 +7,7 @@
 #include <cstddef>
 #include <cstdint>
 
+#include "../../include/gpumultisplit.h"
 #include "gms_device.cuh"
 
 namespace gms {
@@ -98,6 +99,16 @@ template <int KIND>
 cudaError_t run_batch_class(const BatchClassLaunch& c, int stage);
 
 int device_sm_count();
+
+// Batch internals used by the serving runtime: bytes of the plan's tables, and
+// a run that stages the tables through caller-owned pinned memory (at least
+// batch_table_bytes) with one asynchronous copy instead of a synchronous bind.
+size_t batch_table_bytes(gms_batch_t b);
+gms_status batch_run_async(gms_batch_t b, void* d_scratch, size_t scratch_bytes, void* h_pinned,
+                           size_t pinned_bytes, cudaStream_t stream);
+// Index (in uint32 words from the start of the batch scratch) of the scanned
+// offset of (segment, bucket, tile); *base receives the segment's scan base.
+uint32_t batch_matrix_value_offset(gms_batch_t b, uint32_t segment, uint32_t bucket, uint32_t tile, uint32_t* base);
 
 // Records a CUDA error for gms_last_cuda_error() (calling thread).
 void note_cuda_error(cudaError_t e);

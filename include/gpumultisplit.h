@@ -210,6 +210,80 @@ gms_status gms_batch_run(gms_batch_t batch, void* d_scratch, size_t scratch_byte
 gms_status gms_batch_launch_count(gms_batch_t batch, uint32_t* launches);
 gms_status gms_batch_destroy(gms_batch_t batch);
 
+/* -------------------------------------------------------------- serving */
+/* A request loop with continuous batching.  No reference counterpart.  A
+ * scheduler thread admits submitted requests in arrival order while their
+ * memory fits in a caller-provided device arena (the HBM budget), and keeps
+ * launching rounds: each round takes the next step of every admitted request
+ * that is not already on the GPU (a multisplit or compaction is one step, a
+ * 7-bit sort five, one per digit pass) and runs them as one batched multisplit
+ * (plus histogram launches).  Rounds alternate between two streams so the next
+ * round is launched while the previous one is still running; requests that
+ * arrive meanwhile join the next round.  Results live in the arena until
+ * released.  Each result equals the plain call on that request alone. */
+typedef enum gms_op {
+  GMS_OP_MULTISPLIT = 0,  /* stable multisplit, desc as given */
+  GMS_OP_SORT_7BIT = 1,   /* multisplit_sort_7bit[_pairs]; desc ignored */
+  GMS_OP_HISTOGRAM = 2,   /* gms_histogram with desc; values ignored */
+  GMS_OP_COMPACTION = 3   /* compaction with desc (2 buckets); num_bucket0 returned */
+} gms_op;
+
+typedef struct gms_request {
+  int32_t op;                 /* gms_op */
+  const uint32_t* d_key_in;   /* device input, valid until the request is done */
+  const uint32_t* d_value_in; /* null: key-only */
+  uint32_t n;
+  gms_bucket_desc desc;
+} gms_request;
+
+typedef struct gms_result {
+  int32_t done;            /* 1 once finished (then status is final) */
+  int32_t status;          /* gms_status of the request */
+  uint32_t* d_key_out;     /* in the arena: MULTISPLIT, SORT_7BIT, COMPACTION */
+  uint32_t* d_value_out;   /* in the arena, when the request has values */
+  int32_t* d_histogram;    /* in the arena: HISTOGRAM (desc.num_buckets counts) */
+  uint32_t num_bucket0;    /* COMPACTION */
+  uint32_t rounds;         /* rounds the request took part in */
+  double submit_s;         /* server clock, seconds */
+  double admit_s;
+  double done_s;
+} gms_result;
+
+typedef struct gms_server_stats {
+  uint64_t submitted;
+  uint64_t completed;
+  uint64_t rounds;
+  uint64_t launches;       /* kernel launches issued by all rounds */
+  uint64_t keys;           /* keys of completed requests */
+  uint64_t arena_peak_bytes;
+  uint32_t max_requests_in_round;
+} gms_server_stats;
+
+typedef struct gms_server_s* gms_server_t;
+
+/* d_arena: device memory the server may use for outputs and round scratch
+ * (64 GB in the reference serving workload).  The server also creates two
+ * streams, pinned staging buffers and one scheduler thread. */
+gms_status gms_server_create(void* d_arena, size_t arena_bytes, gms_server_t* server);
+/* Queues a request (never blocks on the GPU).  A request larger than the
+ * arena can ever hold is rejected with GMS_ERROR_SCRATCH_TOO_SMALL. */
+gms_status gms_server_submit(gms_server_t server, const gms_request* request, uint64_t* id);
+/* Current state of a request (result->done == 0 while pending). */
+gms_status gms_server_poll(gms_server_t server, uint64_t id, gms_result* result);
+/* Blocks until the request is done. */
+gms_status gms_server_wait(gms_server_t server, uint64_t id, gms_result* result);
+/* Ids of requests finished since the previous call (up to max). */
+gms_status gms_server_take_completed(gms_server_t server, uint64_t* ids, uint32_t max, uint32_t* count);
+/* Frees a finished request's arena memory and forgets it. */
+gms_status gms_server_release(gms_server_t server, uint64_t id);
+/* Blocks until every submitted request is done. */
+gms_status gms_server_drain(gms_server_t server);
+gms_status gms_server_get_stats(gms_server_t server, gms_server_stats* stats);
+/* Seconds since the server was created (the clock of gms_result times). */
+double gms_server_clock(gms_server_t server);
+/* Stops the scheduler (after draining) and frees host resources; the arena stays the caller's. */
+gms_status gms_server_destroy(gms_server_t server);
+
 /* ------------------------------------------------------------ histogram */
 /* Adds the per-bucket counts of d_key_in[0..n) into d_hist[0..B) (the caller
  * zeroes it first, as with the reference's atomicAdd kernels).  Generalises
