@@ -24,6 +24,7 @@ scaling, no collective on the data path); timing is the max over ranks.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -57,6 +58,10 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline time budget")
     p.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
     p.add_argument("--only-batched", action="store_true", help="print only the batched-form summary")
+    p.add_argument("--no-serving", action="store_true", help="skip the serving-form measurement")
+    p.add_argument("--only-serving", action="store_true", help="print only the serving-form summary")
+    p.add_argument("--serve-seconds", type=float, default=3.0)
+    p.add_argument("--serve-rate", type=float, default=20000.0)
     return p.parse_args()
 
 
@@ -257,6 +262,213 @@ def run_batched(dev, reps: int = 3):
     return res
 
 
+def serving_trace(seconds: float, rate: float, seed: int = 5):
+    """Poisson arrivals at `rate`/s for `seconds`; mix 60% multisplit, 20% 7-bit
+    sort, 10% histogram, 10% compaction; sizes log-uniform in [4096, 16M]; half
+    with values; multisplit B in {2, 8, 32, 256} (delta), histogram 256 bins."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=int(rate * seconds * 1.3) + 16)
+    t = np.cumsum(gaps)
+    t = t[t < seconds]
+    m = len(t)
+    sizes = np.exp(rng.uniform(np.log(4096), np.log(16 << 20), m)).astype(np.int64)
+    ops = rng.choice(4, size=m, p=[0.6, 0.2, 0.1, 0.1])
+    kv = rng.random(m) < 0.5
+    buckets = rng.choice([2, 8, 32, 256], size=m)
+    return t, sizes, ops, kv, buckets
+
+
+def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: float = 64.0, verify: int = 24):
+    """Serving form under Poisson arrivals against the plain per-request calls on
+    the same trace: p50/p99 latency (arrival to result) and Gkeys/s."""
+    import torch
+
+    import gpumultisplit_gb300 as gms
+    from gpumultisplit_gb300 import datagen
+    from gpumultisplit_gb300 import serving as srv
+
+    t_arr, sizes, ops, kv, buckets = serving_trace(seconds, rate)
+    m = len(t_arr)
+    pool_n = 1 << 28
+    keys_pool = datagen.uniform_u32(pool_n, 21, device=dev)
+    vals_pool = torch.arange(pool_n, dtype=torch.int32, device=dev)
+    rng = np.random.default_rng(6)
+    offs = (rng.integers(0, pool_n - sizes, m) // 32 * 32).astype(np.int64)
+    names = ["multisplit", "sort7", "histogram", "compaction"]
+
+    def desc_for(i):
+        op = names[ops[i]]
+        if op == "compaction":
+            return gms.test_bucket(1).desc(2), 2
+        if op == "histogram":
+            return gms.delta_bucket().desc(256), 256
+        if op == "sort7":
+            return srv.BucketDesc(), 2
+        return gms.delta_bucket().desc(int(buckets[i])), int(buckets[i])
+
+    reqs = []
+    base_k, base_v = keys_pool.data_ptr(), vals_pool.data_ptr()
+    for i in range(m):
+        d, _ = desc_for(i)
+        has_v = bool(kv[i]) and ops[i] != 2
+        reqs.append(srv.GmsRequest(int(ops[i]), base_k + 4 * int(offs[i]), base_v + 4 * int(offs[i]) if has_v else None,
+                                   int(sizes[i]), d))
+    total_keys = int(sizes.sum())
+
+    # ---- served
+    server = gms.Server(arena_bytes=int(arena_gb * (1 << 30)))
+    lib = srv._lib_server()
+    h = server._h
+    rid = ctypes.c_uint64()
+    res = srv.GmsResult()
+    ids = [0] * m
+    id_index = {}
+    lat = np.zeros(m)
+    done_t = np.zeros(m)
+    sample = set(np.random.default_rng(7).choice(m, size=min(verify, m), replace=False).tolist())
+    kept = {}
+    ids_buf = (ctypes.c_uint64 * 8192)()
+    cnt = ctypes.c_uint32()
+    finished = 0
+
+    def reap():
+        nonlocal finished
+        lib.gms_server_take_completed(h, ids_buf, 8192, ctypes.byref(cnt))
+        for j in range(cnt.value):
+            r = ids_buf[j]
+            i = id_index[r]
+            lib.gms_server_poll(h, r, ctypes.byref(res))
+            lat[i] = res.done_s - res.submit_s
+            done_t[i] = res.done_s
+            if i in sample:
+                kept[i] = server._result(r, res)
+            else:
+                lib.gms_server_release(h, r)
+            finished += 1
+
+    t0 = lib.gms_server_clock(h) + 0.05
+    for i in range(m):
+        target = t0 + t_arr[i]
+        while lib.gms_server_clock(h) < target:
+            pass
+        st = lib.gms_server_submit(h, ctypes.byref(reqs[i]), ctypes.byref(rid))
+        if st != 0:
+            raise RuntimeError(f"submit failed: {st}")
+        ids[i] = rid.value
+        id_index[rid.value] = i
+        server._meta[rid.value] = (names[ops[i]], int(sizes[i]), reqs[i].d_value_in is not None,
+                                   desc_for(i)[1], None)
+        if i % 64 == 0:
+            reap()
+    lib.gms_server_drain(h)
+    while finished < m:
+        reap()
+    stats = server.stats()
+    served_span = float(done_t.max() - t0)
+    # verify the sampled requests against the plain calls alone
+    ok = True
+    for i, r in kept.items():
+        op, n = names[ops[i]], int(sizes[i])
+        kin = keys_pool[offs[i]:offs[i] + n]
+        vin = vals_pool[offs[i]:offs[i] + n] if reqs[i].d_value_in else None
+        ident = gms.test_bucket(1) if op == "compaction" else gms.delta_bucket()
+        ref = _plain_request(gms, op, kin, vin, n, desc_for(i)[1], ident)
+        if op == "histogram":
+            ok &= bool(torch.equal(r.histogram, ref[0]))
+        else:
+            ok &= bool(torch.equal(r.keys, ref[0])) and (vin is None or bool(torch.equal(r.values, ref[1])))
+            if op == "compaction":
+                ok &= r.num_bucket0 == ref[2]
+    for i in kept:
+        server.release(ids[i])
+    server.close()
+
+    # ---- plain per-request calls on the same trace (one stream, in arrival order)
+    plain_lat = np.zeros(m)
+    ctxs = {}
+    kout = torch.empty(16 << 20, dtype=torch.int32, device=dev)
+    vout = torch.empty(16 << 20, dtype=torch.int32, device=dev)
+    hist = torch.empty(256, dtype=torch.int32, device=dev)
+    tp0 = time.perf_counter() + 0.05
+    for i in range(m):
+        target = tp0 + t_arr[i]
+        while time.perf_counter() < target:
+            pass
+        op, n = names[ops[i]], int(sizes[i])
+        kin = keys_pool[offs[i]:offs[i] + n]
+        vin = vals_pool[offs[i]:offs[i] + n] if reqs[i].d_value_in else None
+        _plain_request(gms, op, kin, vin, n, desc_for(i)[1],
+                       gms.test_bucket(1) if op == "compaction" else gms.delta_bucket(), ctxs, kout, vout, hist)
+        torch.cuda.synchronize()
+        plain_lat[i] = time.perf_counter() - tp0 - t_arr[i]
+    plain_span = time.perf_counter() - tp0
+    del keys_pool, vals_pool, kout, vout
+    torch.cuda.empty_cache()
+    return {
+        "workload": f"Poisson arrivals at {rate:.0f}/s for {seconds:.1f} s ({m} requests): 60% multisplit, "
+                    "20% 7-bit sort, 10% histogram, 10% compaction; sizes log-uniform in [4096, 16M]; "
+                    f"half with values; {arena_gb:.0f} GB arena",
+        "requests": m,
+        "keys": total_keys,
+        "served_gkeys": total_keys / served_span / 1e9,
+        "served_p50_ms": float(np.percentile(lat, 50) * 1e3),
+        "served_p99_ms": float(np.percentile(lat, 99) * 1e3),
+        "plain_gkeys": total_keys / plain_span / 1e9,
+        "plain_p50_ms": float(np.percentile(plain_lat, 50) * 1e3),
+        "plain_p99_ms": float(np.percentile(plain_lat, 99) * 1e3),
+        "throughput_vs_plain": (total_keys / served_span) / (total_keys / plain_span),
+        "rounds": int(stats["rounds"]),
+        "max_requests_in_round": int(stats["max_requests_in_round"]),
+        "launches": int(stats["launches"]),
+        "arena_peak_gb": stats["arena_peak_bytes"] / (1 << 30),
+        "verified_identical": bool(ok),
+        "verified_requests": len(kept),
+    }
+
+
+def _plain_request(gms, op, kin, vin, n, B, ident, ctxs=None, kout=None, vout=None, hist=None):
+    """One request through the plain per-call API (contexts cached by shape)."""
+    import torch
+
+    ctxs = {} if ctxs is None else ctxs
+    kv = vin is not None
+    ko = (kout[:n] if kout is not None else torch.empty(n, dtype=torch.int32, device=kin.device))
+    vo = (vout[:n] if vout is not None else torch.empty(n, dtype=torch.int32, device=kin.device)) if kv else None
+    cap = 16 << 20
+    if op == "histogram":
+        h = hist if hist is not None else torch.empty(B, dtype=torch.int32, device=kin.device)
+        h.zero_()
+        gms.multisplit_histogram(kin, n, h, B, ident)
+        return h, None, None
+    if op == "sort7":
+        key = ("sort", kv)
+        if key not in ctxs:
+            ctxs[key] = gms.ms_sort_context()
+            (gms.multisplit_sort_7bit_allocate_pairs if kv else gms.multisplit_sort_7bit_allocate)(cap, ctxs[key])
+        if kv:
+            gms.multisplit_sort_7bit_pairs(kin, ko, vin, vo, n, ctxs[key])
+        else:
+            gms.multisplit_sort_7bit(kin, ko, n, ctxs[key])
+        return ko, vo, None
+    if op == "compaction":
+        key = ("compaction", kv)
+        if key not in ctxs:
+            ctxs[key] = gms.compaction_context()
+            (gms.compaction_allocate_key_value if kv else gms.compaction_allocate_key_only)(cap, ctxs[key])
+        c = (gms.compaction_key_value(kin, vin, ko, vo, n, ctxs[key], ident) if kv
+             else gms.compaction_key_only(kin, ko, n, ctxs[key], ident))
+        return ko, vo, c
+    key = ("ms", B, kv)
+    if key not in ctxs:
+        ctxs[key] = gms.multisplit_context(B)
+        (gms.multisplit_allocate_key_value if kv else gms.multisplit_allocate_key_only)(cap, ctxs[key])
+    if kv:
+        gms.multisplit_key_value(kin, vin, ko, vo, n, ctxs[key], ident)
+    else:
+        gms.multisplit_key_only(kin, ko, n, ctxs[key], ident)
+    return ko, vo, None
+
+
 def cpu_baseline(a, keys_dev, vals_dev, seconds):
     """Times the oracle's multi-threaded restatement on a bounded sample."""
     import oracle
@@ -328,11 +540,12 @@ def run_ours(a):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if a.only_batched:
+    if a.only_batched or a.only_serving:
         from gpumultisplit_gb300 import build as gbuild
 
         gbuild.build()
-        print(json.dumps(run_batched(dev)), flush=True)
+        out = run_batched(dev) if a.only_batched else run_serving(dev, a.serve_seconds, a.serve_rate)
+        print(json.dumps(out), flush=True)
         return
     if world > 1:
         import torch.distributed as dist
@@ -464,6 +677,8 @@ def run_ours(a):
         del keys, vals, kout, vout
         torch.cuda.empty_cache()
         line["batched"] = run_batched(dev)
+    if not a.no_serving:
+        line["serving"] = run_serving(dev, a.serve_seconds, a.serve_rate)
     if rank == 0 and not a.no_cpu_baseline:
         keys, vals, _ = make_inputs(a, dev)
         line["cpu_baseline"] = cpu_baseline(a, keys, vals, a.cpu_seconds)
