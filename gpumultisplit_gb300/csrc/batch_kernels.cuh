@@ -34,14 +34,15 @@ __global__ void __launch_bounds__(C::THREADS) batch_prescan_kernel(const SegDesc
                                                                    const uint2* __restrict__ tile_map,
                                                                    uint32_t class_tiles,
                                                                    uint32_t* __restrict__ matrix) {
-  using Counter = KeyCounter<C::LOGB, KIND>;
+  using P = DescPolicy<KIND, C::LOGB>;
+  using Counter = KeyCounter<C::LOGB, typename P::Id>;
   __shared__ uint32_t s_hist[Counter::smem_words(C::WARPS)];
-  __shared__ uint32_t s_split[identifier_smem_words<KIND, C::LOGB>()];
+  __shared__ uint32_t s_split[P::SMEM_WORDS];
   const uint32_t tid = threadIdx.x;
 
   SegDesc sd{};
   uint32_t cur = ~0u;
-  Counter counter(Identifier<KIND, C::LOGB>{BucketParams{}, s_split}, s_hist);
+  Counter counter(P::make(BucketParams{}, s_split), s_hist);
   counter.clear_shared();
   __syncthreads();
   for (uint32_t t = blockIdx.x; t < class_tiles; t += gridDim.x) {
@@ -49,9 +50,9 @@ __global__ void __launch_bounds__(C::THREADS) batch_prescan_kernel(const SegDesc
     if (m.x != cur) {
       cur = m.x;
       sd = segs[cur];
-      prepare_identifier<KIND, C::LOGB>(s_split, sd.bp);
-      if constexpr (KIND == KIND_RANGE) __syncthreads();
-      counter.ident = Identifier<KIND, C::LOGB>{sd.bp, s_split};
+      P::prepare(s_split, sd.bp);
+      if constexpr (P::USES_SMEM) __syncthreads();
+      counter.ident = P::make(sd.bp, s_split);
     }
     const uint32_t base = m.y * C::TILE;
     const uint32_t cnt = min(C::TILE, sd.n - base);
@@ -74,25 +75,15 @@ __global__ void __launch_bounds__(C::THREADS) batch_prescan_kernel(const SegDesc
 
 // One block per tile of one class.
 template <class C, int KIND>
-__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, KIND>::MIN_BLOCKS))
+__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, DescPolicy<KIND, C::LOGB>>::MIN_BLOCKS))
     batch_postscan_kernel(const SegDesc* __restrict__ segs, const uint2* __restrict__ tile_map,
                           const uint32_t* __restrict__ matrix, ScratchHeader* hdr) {
   extern __shared__ __align__(128) unsigned char smem[];
   const uint2 m = tile_map[blockIdx.x];
   const SegDesc& sd = segs[m.x];
-  TileJob job;
-  job.kin = sd.kin;
-  job.vin = sd.vin;
-  job.kout = sd.kout;
-  job.vout = sd.vout;
-  job.n = sd.n;
-  job.num_tiles = sd.num_tiles;
-  job.tile = m.y;
-  job.offsets = matrix + sd.matrix_off;
-  job.bias = sd.base;
-  job.prefetch_tile = ~0u;
-  job.bp = sd.bp;
-  postscan_job<C, KIND>(job, hdr, smem);
+  const TileJob<BucketParams> job{sd.kin, sd.vin,  sd.kout, sd.vout, sd.n,  sd.num_tiles,
+                                  m.y,    matrix + sd.matrix_off, sd.base, ~0u, sd.bp};
+  postscan_job<C, DescPolicy<KIND, C::LOGB>>(job, hdr, smem);
 }
 
 }  // namespace gms

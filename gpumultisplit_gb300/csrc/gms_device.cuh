@@ -229,4 +229,40 @@ __device__ __forceinline__ void prepare_identifier(uint32_t* s_split, const Buck
   }
 }
 
+// Identifier policies: what the kernels need to know about a bucket
+// identifier.  DescPolicy covers the precompiled descriptor kinds; the drop-in
+// C++ headers use FunctorPolicy to instantiate the same kernels with any
+// device-callable functor, compiled in the caller's translation unit.
+template <int KIND, int LOGB>
+struct DescPolicy {
+  using Params = BucketParams;
+  using Id = Identifier<KIND, LOGB>;
+  static constexpr bool CHEAP = KIND == KIND_DELTA || KIND == KIND_BITS || KIND == KIND_MASK;
+  static constexpr bool USES_SMEM = KIND == KIND_RANGE;
+  static constexpr uint32_t SMEM_WORDS = identifier_smem_words<KIND, LOGB>();
+  __device__ __forceinline__ static void prepare(uint32_t* s, const Params& p) { prepare_identifier<KIND, LOGB>(s, p); }
+  __device__ __forceinline__ static Id make(const Params& p, const uint32_t* s) { return Id{p, s}; }
+};
+
+// A user functor (operator() on a 32-bit key, returning the bucket); its
+// value is reduced modulo B like every other identifier.
+template <class F, int LOGB>
+struct FunctorId {
+  F f;
+  __device__ __forceinline__ uint32_t operator()(uint32_t key) const {
+    return uint32_t(f(key)) & ((1u << LOGB) - 1u);
+  }
+};
+
+template <class F, int LOGB>
+struct FunctorPolicy {
+  using Params = F;
+  using Id = FunctorId<F, LOGB>;
+  static constexpr bool CHEAP = false;  // cost unknown: buckets are computed once per key and kept
+  static constexpr bool USES_SMEM = false;
+  static constexpr uint32_t SMEM_WORDS = 1;
+  __device__ __forceinline__ static void prepare(uint32_t*, const Params&) {}
+  __device__ __forceinline__ static Id make(const Params& f, const uint32_t*) { return Id{f}; }
+};
+
 }  // namespace gms

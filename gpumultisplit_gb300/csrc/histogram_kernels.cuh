@@ -17,15 +17,14 @@ constexpr int HIST_IPT = 16;
 constexpr uint32_t HIST_CHUNK = HIST_THREADS * HIST_IPT;
 
 // Persistent grid; block-strided over chunks of HIST_CHUNK keys.
-template <int LOGB, int KIND>
+template <int LOGB, class P>
 __global__ void __launch_bounds__(HIST_THREADS) histogram_kernel(const uint32_t* __restrict__ keys, uint32_t n,
-                                                                 int32_t* __restrict__ hist, BucketParams bp) {
-  using Counter = KeyCounter<LOGB, KIND>;
+                                                                 int32_t* __restrict__ hist, typename P::Params bp) {
+  using Counter = KeyCounter<LOGB, typename P::Id>;
   __shared__ uint32_t s_hist[Counter::smem_words(HIST_WARPS)];
-  __shared__ uint32_t s_split[identifier_smem_words<KIND, LOGB>()];
-  prepare_identifier<KIND, LOGB>(s_split, bp);
-  const Identifier<KIND, LOGB> ident{bp, s_split};
-  Counter counter(ident, s_hist);
+  __shared__ uint32_t s_split[P::SMEM_WORDS];
+  P::prepare(s_split, bp);
+  Counter counter(P::make(bp, s_split), s_hist);
   counter.clear_shared();
   __syncthreads();
   count_tiles<HIST_THREADS, HIST_IPT>(keys, n, blockIdx.x, gridDim.x, counter, [](uint32_t) {});

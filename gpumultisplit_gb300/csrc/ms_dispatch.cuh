@@ -47,44 +47,55 @@ inline uint32_t persistent_grid(Kernel k, int threads, uint32_t work, std::atomi
   return uint32_t(work < cap ? work : cap);
 }
 
-template <int KIND, int LOGB, bool KV>
-cudaError_t run_multisplit_t(const MsCall& c, int stages) {
+// Stages of one multisplit with identifier policy P (descriptor kinds here;
+// user functors from the drop-in C++ headers).  `scratch` is laid out as
+// make_geometry(n, LOGB, KV).
+template <class P, int LOGB, bool KV>
+cudaError_t launch_multisplit(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n,
+                              const typename P::Params& params, unsigned char* scratch, int stages,
+                              cudaStream_t stream) {
   using S = TileShape<LOGB, KV>;
   using C = TileCfg<LOGB, S::WARPS, S::IPT, KV>;
-  const Geometry g = make_geometry(c.n, LOGB, KV);
+  const Geometry g = make_geometry(n, LOGB, KV);
   if (g.num_tiles == 0) return cudaSuccess;
-  auto* hdr = reinterpret_cast<ScratchHeader*>(c.scratch);
-  auto* status = reinterpret_cast<uint64_t*>(c.scratch + g.off_status);
-  auto* matrix = reinterpret_cast<uint32_t*>(c.scratch + g.off_matrix);
+  auto* hdr = reinterpret_cast<ScratchHeader*>(scratch);
+  auto* status = reinterpret_cast<uint64_t*>(scratch + g.off_status);
+  auto* matrix = reinterpret_cast<uint32_t*>(scratch + g.off_matrix);
 
   if (stages & STAGE_PRESCAN) {
     static std::atomic<int> per_sm{0};
-    auto kern = prescan_kernel<C, KIND>;
+    auto kern = prescan_kernel<C, P>;
     const uint32_t grid = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm);
-    kern<<<grid, C::THREADS, 0, c.stream>>>(c.kin, c.n, g.num_tiles, matrix, c.bp, hdr, status, g.num_chunks);
+    kern<<<grid, C::THREADS, 0, stream>>>(kin, n, g.num_tiles, matrix, params, hdr, status, g.num_chunks);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   if (stages & STAGE_SCAN) {
-    cudaError_t e = run_scan(matrix, g.m, status, hdr, c.stream);
+    cudaError_t e = run_scan(matrix, g.m, status, hdr, stream);
     if (e != cudaSuccess) return e;
   }
   if (stages & STAGE_POSTSCAN) {
     static std::atomic<uint64_t> smem_done{0};
     static std::atomic<int> per_sm{0};
-    auto kern = postscan_kernel<C, KIND>;
-    constexpr size_t smem = PostLayout<C, KIND>::BYTES;
+    auto kern = postscan_kernel<C, P>;
+    constexpr size_t smem = PostLayout<C, P>::BYTES;
     cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
     if (e != cudaSuccess) return e;
-    // Prefetch distance: the number of blocks resident at once (one wave).
+    // Prefetch distance: a fraction of the number of blocks resident at once (one wave).
     const uint32_t wave = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
     const uint32_t dist = (GMS_PREFETCH_WAVES * wave) / 4u;
-    kern<<<g.num_tiles, C::THREADS, smem, c.stream>>>(c.kin, c.vin, c.kout, c.vout, c.n, g.num_tiles, matrix,
-                                                             c.bp, hdr, dist);
+    kern<<<g.num_tiles, C::THREADS, smem, stream>>>(kin, vin, kout, vout, n, g.num_tiles, matrix, params, hdr,
+                                                      dist);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+template <int KIND, int LOGB, bool KV>
+cudaError_t run_multisplit_t(const MsCall& c, int stages) {
+  return launch_multisplit<DescPolicy<KIND, LOGB>, LOGB, KV>(c.kin, c.vin, c.kout, c.vout, c.n, c.bp, c.scratch,
+                                                             stages, c.stream);
 }
 
 template <int KIND, bool KV>
@@ -121,7 +132,7 @@ cudaError_t run_batch_class_t(const BatchClassLaunch& c, int stage) {
   }
   static std::atomic<uint64_t> smem_done{0};
   auto kern = batch_postscan_kernel<C, KIND>;
-  constexpr size_t smem = PostLayout<C, KIND>::BYTES;
+  constexpr size_t smem = PostLayout<C, DescPolicy<KIND, LOGB>>::BYTES;
   cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
   if (e != cudaSuccess) return e;
   kern<<<c.class_tiles, C::THREADS, smem, c.stream>>>(c.segs, c.tile_map, c.matrix, c.hdr);
@@ -153,7 +164,7 @@ cudaError_t run_histogram_t(const uint32_t* keys, uint32_t n, const BucketParams
                             cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   static std::atomic<int> per_sm{0};
-  auto kern = histogram_kernel<LOGB, KIND>;
+  auto kern = histogram_kernel<LOGB, DescPolicy<KIND, LOGB>>;
   const uint32_t grid = persistent_grid(kern, HIST_THREADS, (n + HIST_CHUNK - 1) / HIST_CHUNK, per_sm);
   kern<<<grid, HIST_THREADS, 0, stream>>>(keys, n, hist, bp);
   return cudaGetLastError();

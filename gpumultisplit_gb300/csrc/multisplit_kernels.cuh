@@ -62,19 +62,19 @@ struct TileCfg {
 #define GMS_COUNT_BALLOT_MAX_LOGB 0
 #endif
 
-template <int LOGB, int KIND>
+template <int LOGB, class Id>
 struct KeyCounter {
   static constexpr uint32_t B = 1u << LOGB;
   static constexpr bool kBallot = LOGB <= GMS_COUNT_BALLOT_MAX_LOGB;
   static constexpr uint32_t R = B >= 32 ? 1u : 32u / B;  // histogram replicas (atomic path)
   static constexpr uint32_t HIST_WORDS = B * R;         // >= 32
-  Identifier<KIND, LOGB> ident;
+  Id ident;
   uint32_t* s_hist;                      // HIST_WORDS (atomic path) or WARPS*32 (ballot path)
   uint32_t acc[4] = {0u, 0u, 0u, 0u};    // ballot path: independent accumulators keep the chains parallel
   uint32_t xm[kBallot ? LOGB : 1];
   uint32_t slot;                          // atomic path: this lane's replica offset
 
-  __device__ __forceinline__ KeyCounter(const Identifier<KIND, LOGB>& id, uint32_t* hist) : ident(id), s_hist(hist) {
+  __device__ __forceinline__ KeyCounter(const Id& id, uint32_t* hist) : ident(id), s_hist(hist) {
     const uint32_t lane = lane_id();
     if constexpr (kBallot) {
 #pragma unroll
@@ -191,14 +191,14 @@ __device__ __forceinline__ void count_tiles(const uint32_t* __restrict__ keys, u
 // Persistent grid over the tiles.  Writes counts[b * num_tiles + tile] for
 // every tile and resets the scan state (ticket, chunk status words, error
 // word) for the scan that follows.
-template <class C, int KIND>
+template <class C, class P>
 __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __restrict__ keys, uint32_t n,
                                                              uint32_t num_tiles, uint32_t* __restrict__ counts,
-                                                             BucketParams bp, ScratchHeader* hdr,
+                                                             typename P::Params bp, ScratchHeader* hdr,
                                                              uint64_t* __restrict__ status, uint32_t num_chunks) {
-  using Counter = KeyCounter<C::LOGB, KIND>;
+  using Counter = KeyCounter<C::LOGB, typename P::Id>;
   __shared__ uint32_t s_hist[Counter::smem_words(C::WARPS)];
-  __shared__ uint32_t s_split[identifier_smem_words<KIND, C::LOGB>()];  // RANGE splitters + table
+  __shared__ uint32_t s_split[P::SMEM_WORDS];  // identifier state (RANGE splitters + table)
 
   const uint32_t tid = threadIdx.x;
 
@@ -210,9 +210,8 @@ __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __r
     hdr->ticket = 0u;
   }
 
-  prepare_identifier<KIND, C::LOGB>(s_split, bp);
-  Identifier<KIND, C::LOGB> ident{bp, s_split};
-  Counter counter(ident, s_hist);
+  P::prepare(s_split, bp);
+  Counter counter(P::make(bp, s_split), s_hist);
   counter.clear_shared();
   __syncthreads();
   count_tiles<C::THREADS, C::IPT>(keys, n, blockIdx.x, gridDim.x, counter, [&](uint32_t tile) {
@@ -231,9 +230,9 @@ __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __r
 //              recompute (RANGE, DIV, EVEN_FLOAT).
 enum ReorderMode { R_KEYS = 0, R_INDEX16 = 1, R_PACKED = 2 };
 
-template <class C, int KIND>
+template <class C, class P>
 struct PostLayout {
-  static constexpr bool CHEAP = KIND == KIND_DELTA || KIND == KIND_BITS || KIND == KIND_MASK;
+  static constexpr bool CHEAP = P::CHEAP;
   static constexpr int MODE = !CHEAP ? R_PACKED : (C::KV ? R_INDEX16 : R_KEYS);
   static constexpr size_t OFF_K = 0;
   static constexpr size_t OFF_V = OFF_K + C::TILE * 4;
@@ -242,7 +241,7 @@ struct PostLayout {
   static constexpr size_t OFF_WH = (OFF_R + R_BYTES + 15) & ~size_t(15);
   static constexpr size_t OFF_DELTA = OFF_WH + size_t(C::WARPS) * C::WB * C::WS * 4;
   static constexpr size_t OFF_SPLIT = OFF_DELTA + C::B * 4;
-  static constexpr size_t OFF_SCAN = OFF_SPLIT + identifier_smem_words<KIND, C::LOGB>() * 4;
+  static constexpr size_t OFF_SCAN = OFF_SPLIT + P::SMEM_WORDS * 4;
   static constexpr size_t OFF_FLAG = OFF_SCAN + C::B * 4;
   static constexpr size_t OFF_BAR = (OFF_FLAG + 4 + 15) & ~size_t(15);
   static constexpr size_t BYTES = OFF_BAR + 16;
@@ -267,11 +266,11 @@ __device__ __forceinline__ uint32_t peers_by_ballot(uint32_t b) {
 
 // Phases 1-4 of the postscan for one staged tile.  FULL: the tile holds
 // exactly TILE keys, so no per-key validity test is needed.
-template <class C, int KIND, bool FULL>
+template <class C, class P, bool FULL>
 __device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
-                                              uint32_t cnt, uint32_t goff, const BucketParams& bp, ScratchHeader* hdr,
-                                              unsigned char* smem) {
-  using L = PostLayout<C, KIND>;
+                                              uint32_t cnt, uint32_t goff, const typename P::Params& bp,
+                                              ScratchHeader* hdr, unsigned char* smem) {
+  using L = PostLayout<C, P>;
   constexpr uint32_t B = C::B;
   constexpr int LOGB = C::LOGB;
   constexpr int IPT = C::IPT;
@@ -290,7 +289,7 @@ __device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint3
   const uint32_t warp = tid >> 5;
 
   // ---- 1. stable in-warp ranks
-  const Identifier<KIND, LOGB> ident{bp, s_split};
+  const typename P::Id ident = P::make(bp, s_split);
   uint32_t packed[IPT];  // (bucket << 16) | rank among same-bucket keys of this warp
   const uint32_t wbase = warp * (IPT * 32u);
   const uint32_t lt = lanemask_lt();
@@ -445,6 +444,7 @@ __device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint3
 
 // -------------------------------------------------------------- postscan
 // One tile of one multisplit, as the postscan sees it.
+template <class Params>
 struct TileJob {
   const uint32_t* kin;
   const uint32_t* vin;
@@ -456,7 +456,7 @@ struct TileJob {
   const uint32_t* offsets;   // its scanned count matrix, bucket-major
   uint32_t bias;             // subtracted from the scanned offsets (start of this multisplit in a shared scan)
   uint32_t prefetch_tile;    // a later tile of the same arrays to pull into L2 (>= num_tiles: none)
-  BucketParams bp;
+  Params bp;
 };
 
 // Postscan of one tile, run by a whole block:
@@ -470,9 +470,10 @@ struct TileJob {
 //  3. write, at each key's bucket-sorted in-tile position, its key or source index;
 //  4. walk the bucket-sorted order: out[delta[b] + p] = key (value), so every
 //     bucket's run is a contiguous, coalesced store.
-template <class C, int KIND>
-__device__ __forceinline__ void postscan_job(const TileJob& job, ScratchHeader* hdr, unsigned char* smem) {
-  using L = PostLayout<C, KIND>;
+template <class C, class P>
+__device__ __forceinline__ void postscan_job(const TileJob<typename P::Params>& job, ScratchHeader* hdr,
+                                             unsigned char* smem) {
+  using L = PostLayout<C, P>;
   constexpr uint32_t B = C::B;
   constexpr int LOGB = C::LOGB;
   constexpr uint32_t WB = C::WB;
@@ -511,7 +512,7 @@ __device__ __forceinline__ void postscan_job(const TileJob& job, ScratchHeader* 
     if constexpr (C::KV) s_v[i] = vin[base + i];
   }
   const uint32_t goff = (tid < B) ? job.offsets[tid * job.num_tiles + job.tile] - job.bias : 0u;
-  prepare_identifier<KIND, LOGB>(s_split, job.bp);
+  P::prepare(s_split, job.bp);
   if constexpr (LOGB > 5) {
     for (uint32_t i = tid; i < C::WARPS * WB * C::WS; i += C::THREADS) s_wh[i] = 0u;
   }
@@ -528,31 +529,23 @@ __device__ __forceinline__ void postscan_job(const TileJob& job, ScratchHeader* 
   }
 
   if (cnt == C::TILE)
-    postscan_tile<C, KIND, true>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
+    postscan_tile<C, P, true>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
   else
-    postscan_tile<C, KIND, false>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
+    postscan_tile<C, P, false>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
 }
 
 // Plain postscan: one block per tile of one multisplit.
-template <class C, int KIND>
-__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, KIND>::MIN_BLOCKS)) postscan_kernel(
+template <class C, class P>
+__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P>::MIN_BLOCKS)) postscan_kernel(
     const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
     uint32_t* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
-    BucketParams bp, ScratchHeader* hdr, uint32_t prefetch_dist) {
+    typename P::Params bp, ScratchHeader* hdr, uint32_t prefetch_dist) {
   extern __shared__ __align__(128) unsigned char smem[];
-  TileJob job;
-  job.kin = kin;
-  job.vin = vin;
-  job.kout = kout;
-  job.vout = vout;
-  job.n = n;
-  job.num_tiles = num_tiles;
-  job.tile = blockIdx.x;
-  job.offsets = offsets;
-  job.bias = 0u;
-  job.prefetch_tile = prefetch_dist != 0 ? blockIdx.x + prefetch_dist : ~0u;
-  job.bp = bp;
-  postscan_job<C, KIND>(job, hdr, smem);
+  const TileJob<typename P::Params> job{kin,        vin,     kout, vout,
+                                        n,          num_tiles, blockIdx.x, offsets,
+                                        0u,         prefetch_dist != 0 ? blockIdx.x + prefetch_dist : ~0u,
+                                        bp};
+  postscan_job<C, P>(job, hdr, smem);
 }
 
 }  // namespace gms
