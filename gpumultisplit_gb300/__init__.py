@@ -38,5 +38,11 @@ from .api import (  # noqa: F401
     test_bucket,
 )
 from ._lib import GmsError, load  # noqa: F401
+from .api import (  # noqa: F401
+    multisplit_sort_4bit, multisplit_sort_4bit_allocate, multisplit_sort_4bit_allocate_pairs, multisplit_sort_4bit_pairs,
+    multisplit_sort_5bit, multisplit_sort_5bit_allocate, multisplit_sort_5bit_allocate_pairs, multisplit_sort_5bit_pairs,
+    multisplit_sort_6bit, multisplit_sort_6bit_allocate, multisplit_sort_6bit_allocate_pairs, multisplit_sort_6bit_pairs,
+    multisplit_sort_8bit, multisplit_sort_8bit_allocate, multisplit_sort_8bit_allocate_pairs, multisplit_sort_8bit_pairs,
+)
 from .batched import BatchedMultisplit, Segment  # noqa: F401
 from .serving import Result, Server  # noqa: F401

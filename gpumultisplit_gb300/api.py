@@ -310,12 +310,24 @@ class ms_sort_context:
         self.temp_storage_bytes = 0
 
 
-def _sort_allocate(n_elements, context, key_value):
+def _sort_allocate(n_elements, context, key_value, digit_bits=7):
     nbytes = ctypes.c_size_t()
-    check(_lib.load().gms_sort_7bit_scratch_bytes(n_elements, int(key_value), ctypes.byref(nbytes)),
-          "multisplit_sort_7bit_allocate")
+    check(_lib.load().gms_sort_scratch_bytes(n_elements, digit_bits, int(key_value), ctypes.byref(nbytes)),
+          f"multisplit_sort_{digit_bits}bit_allocate")
     context.temp_storage_bytes = nbytes.value
     context.d_temp_storage = _alloc_scratch(nbytes.value)
+    context.digit_bits = digit_bits
+
+
+def _sort_run(d_key_in, d_key_out, d_value_in, d_value_out, n, context, digit_bits, stream):
+    lib = _lib.load()
+    if d_value_in is None:
+        st = lib.gms_sort_key_only(_ptr(d_key_in), _ptr(d_key_out), n, digit_bits, _scratch(context),
+                                   context.temp_storage_bytes, _stream(stream))
+    else:
+        st = lib.gms_sort_key_value(_ptr(d_key_in), _ptr(d_key_out), _ptr(d_value_in), _ptr(d_value_out), n,
+                                    digit_bits, _scratch(context), context.temp_storage_bytes, _stream(stream))
+    check(st, f"multisplit_sort_{digit_bits}bit")
 
 
 def multisplit_sort_7bit_allocate(n_elements: int, context: ms_sort_context) -> None:
@@ -348,6 +360,33 @@ def multisplit_sort_7bit_pairs(d_key_in, d_key_out_ms, d_value_in, d_value_out_m
                                               _ptr(d_value_out_ms), n_elements, _scratch(context),
                                               context.temp_storage_bytes, _stream(stream)),
           "multisplit_sort_7bit_pairs")
+
+
+def _define_sorts(bits: int):
+    """multisplit_sort_<bits>bit[_allocate][_pairs] (src/api/multisplit_sort.cuh:118-559,
+    src/api/multisplit_sort_pairs.cuh:67-260)."""
+
+    def allocate(n_elements, context):
+        _sort_allocate(n_elements, context, False, bits)
+
+    def allocate_pairs(n_elements, context):
+        _sort_allocate(n_elements, context, True, bits)
+
+    def sort(d_key_in, d_key_out_ms, n_elements, context, stream=None):
+        _sort_run(d_key_in, d_key_out_ms, None, None, n_elements, context, bits, stream)
+
+    def sort_pairs(d_key_in, d_key_out_ms, d_value_in, d_value_out_ms, n_elements, context, stream=None):
+        _sort_run(d_key_in, d_key_out_ms, d_value_in, d_value_out_ms, n_elements, context, bits, stream)
+
+    g = globals()
+    g[f"multisplit_sort_{bits}bit_allocate"] = allocate
+    g[f"multisplit_sort_{bits}bit_allocate_pairs"] = allocate_pairs
+    g[f"multisplit_sort_{bits}bit"] = sort
+    g[f"multisplit_sort_{bits}bit_pairs"] = sort_pairs
+
+
+for _bits in (4, 5, 6, 8):
+    _define_sorts(_bits)
 
 
 # -------------------------------------------------------------- compaction

@@ -139,54 +139,79 @@ gms_status copy_offsets(const void* scratch, uint32_t n, int logb, bool kv, uint
   return cuda_status(e);
 }
 
+// Digit schedules of the reference's multisplit sorts
+// (src/api/multisplit_sort.cuh:320-559, src/api/multisplit_sort_pairs.cuh:21-260):
+// (shift, buckets) per pass, least significant digit first.
+struct SortSchedule {
+  int passes;
+  uint32_t shift[8];
+  uint32_t buckets[8];
+};
+
+bool sort_schedule(int digit_bits, SortSchedule* s) {
+  switch (digit_bits) {
+    case 4: *s = {8, {0, 4, 8, 12, 16, 20, 24, 28}, {16, 16, 16, 16, 16, 16, 16, 16}}; return true;
+    case 5: *s = {7, {0, 5, 10, 15, 20, 25, 30}, {32, 32, 32, 32, 32, 32, 4}}; return true;
+    case 6: *s = {6, {0, 4, 8, 14, 20, 26}, {16, 16, 64, 64, 64, 64}}; return true;
+    case 7: *s = {5, {0, 4, 11, 18, 25}, {16, 128, 128, 128, 128}}; return true;
+    case 8: *s = {4, {0, 8, 16, 24}, {256, 256, 256, 256}}; return true;
+    default: return false;
+  }
+}
+
 struct SortLayout {
-  size_t ms_bytes;   // multisplit scratch (largest of the two digit widths)
+  size_t ms_bytes;   // multisplit scratch (largest over the schedule's digit widths)
   size_t off_keys;   // ping-pong keys
   size_t off_vals;   // ping-pong values
   size_t bytes;
 };
 
-SortLayout sort_layout(uint32_t n, bool kv) {
+SortLayout sort_layout(uint32_t n, bool kv, const SortSchedule& sch) {
   SortLayout L;
-  const Geometry g4 = make_geometry(n, 4, kv), g7 = make_geometry(n, 7, kv);
-  L.ms_bytes = g4.bytes > g7.bytes ? g4.bytes : g7.bytes;
+  L.ms_bytes = 0;
+  for (int p = 0; p < sch.passes; ++p) {
+    int logb = 0;
+    valid_buckets(sch.buckets[p], &logb);
+    const size_t b = make_geometry(n, logb, kv).bytes;
+    L.ms_bytes = b > L.ms_bytes ? b : L.ms_bytes;
+  }
   L.off_keys = align_up(L.ms_bytes, 256);
   L.off_vals = align_up(L.off_keys + size_t(n) * 4, 256);
   L.bytes = kv ? align_up(L.off_vals + size_t(n) * 4, 256) : L.off_vals;
   return L;
 }
 
+// LSD radix sort by stable multisplits on successive digits.  The buffers
+// ping-pong between the output and the scratch copy so the last pass lands in
+// the output (an odd number of passes starts in the output, an even one in the
+// copy), and the input is never written.
 gms_status sort_impl(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
-                     bool kv, void* scratch, size_t scratch_bytes, cudaStream_t stream) {
+                     bool kv, int digit_bits, void* scratch, size_t scratch_bytes, cudaStream_t stream) {
+  SortSchedule sch;
+  if (!sort_schedule(digit_bits, &sch)) return GMS_ERROR_INVALID_VALUE;
   if (n == 0) return GMS_SUCCESS;
   if (kin == nullptr || kout == nullptr || scratch == nullptr) return GMS_ERROR_INVALID_VALUE;
   if (kv && (vin == nullptr || vout == nullptr)) return GMS_ERROR_INVALID_VALUE;
-  const SortLayout L = sort_layout(n, kv);
+  const SortLayout L = sort_layout(n, kv, sch);
   if (scratch_bytes < L.bytes) return GMS_ERROR_SCRATCH_TOO_SMALL;
   auto* base = static_cast<unsigned char*>(scratch);
   uint32_t* tk = reinterpret_cast<uint32_t*>(base + L.off_keys);
   uint32_t* tv = kv ? reinterpret_cast<uint32_t*>(base + L.off_vals) : nullptr;
-
-  // Digit schedule and buffer ping-pong of src/api/multisplit_sort.cuh:333-363.
-  struct Pass {
-    uint32_t shift, buckets;
-    const uint32_t *ki, *vi;
-    uint32_t *ko, *vo;
-  };
-  const Pass passes[5] = {{0, 16, kin, vin, kout, vout},
-                          {4, 128, kout, vout, tk, tv},
-                          {11, 128, tk, tv, kout, vout},
-                          {18, 128, kout, vout, tk, tv},
-                          {25, 128, tk, tv, kout, vout}};
-  for (const Pass& p : passes) {
+  const uint32_t* ki = kin;
+  const uint32_t* vi = vin;
+  for (int p = 0; p < sch.passes; ++p) {
+    const bool to_out = ((sch.passes - 1 - p) % 2) == 0;
+    uint32_t* ko = to_out ? kout : tk;
+    uint32_t* vo = to_out ? vout : tv;
     gms_bucket_desc d{};
     d.kind = GMS_BUCKET_BITS;
-    d.num_buckets = p.buckets;
-    d.shift = p.shift;
-    gms_status st =
-        multisplit_impl(p.ki, kv ? p.vi : nullptr, p.ko, kv ? p.vo : nullptr, n, &d, kv, scratch, L.ms_bytes,
-                        STAGE_ALL, stream);
+    d.num_buckets = sch.buckets[p];
+    d.shift = sch.shift[p];
+    gms_status st = multisplit_impl(ki, kv ? vi : nullptr, ko, kv ? vo : nullptr, n, &d, kv, scratch, L.ms_bytes,
+                                    STAGE_ALL, stream);
     if (st != GMS_SUCCESS) return st;
+    ki = ko;
+    vi = vo;
   }
   return GMS_SUCCESS;
 }
@@ -342,21 +367,38 @@ gms_status gms_multisplit_postscan(const uint32_t* d_key_in, const uint32_t* d_v
                          scratch_bytes, STAGE_POSTSCAN, stream);
 }
 
-gms_status gms_sort_7bit_scratch_bytes(uint32_t max_elements, int key_value, size_t* bytes) {
-  if (bytes == nullptr) return GMS_ERROR_INVALID_VALUE;
-  *bytes = sort_layout(max_elements, key_value != 0).bytes;
+gms_status gms_sort_scratch_bytes(uint32_t max_elements, int digit_bits, int key_value, size_t* bytes) {
+  SortSchedule sch;
+  if (bytes == nullptr || !sort_schedule(digit_bits, &sch)) return GMS_ERROR_INVALID_VALUE;
+  *bytes = sort_layout(max_elements, key_value != 0, sch).bytes;
   return GMS_SUCCESS;
+}
+
+gms_status gms_sort_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n, int digit_bits,
+                             void* d_scratch, size_t scratch_bytes, gms_stream_t stream) {
+  return sort_impl(d_key_in, d_key_out, nullptr, nullptr, n, false, digit_bits, d_scratch, scratch_bytes, stream);
+}
+
+gms_status gms_sort_key_value(const uint32_t* d_key_in, uint32_t* d_key_out, const uint32_t* d_value_in,
+                              uint32_t* d_value_out, uint32_t n, int digit_bits, void* d_scratch,
+                              size_t scratch_bytes, gms_stream_t stream) {
+  return sort_impl(d_key_in, d_key_out, d_value_in, d_value_out, n, true, digit_bits, d_scratch, scratch_bytes,
+                   stream);
+}
+
+gms_status gms_sort_7bit_scratch_bytes(uint32_t max_elements, int key_value, size_t* bytes) {
+  return gms_sort_scratch_bytes(max_elements, 7, key_value, bytes);
 }
 
 gms_status gms_sort_7bit_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n, void* d_scratch,
                                   size_t scratch_bytes, gms_stream_t stream) {
-  return sort_impl(d_key_in, d_key_out, nullptr, nullptr, n, false, d_scratch, scratch_bytes, stream);
+  return gms_sort_key_only(d_key_in, d_key_out, n, 7, d_scratch, scratch_bytes, stream);
 }
 
 gms_status gms_sort_7bit_key_value(const uint32_t* d_key_in, uint32_t* d_key_out, const uint32_t* d_value_in,
                                    uint32_t* d_value_out, uint32_t n, void* d_scratch, size_t scratch_bytes,
                                    gms_stream_t stream) {
-  return sort_impl(d_key_in, d_key_out, d_value_in, d_value_out, n, true, d_scratch, scratch_bytes, stream);
+  return gms_sort_key_value(d_key_in, d_key_out, d_value_in, d_value_out, n, 7, d_scratch, scratch_bytes, stream);
 }
 
 gms_status gms_compaction_scratch_bytes(uint32_t max_elements, int key_value, size_t* bytes) {

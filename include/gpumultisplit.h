@@ -160,6 +160,19 @@ gms_status gms_sort_7bit_key_value(const uint32_t* d_key_in, uint32_t* d_key_out
                                    uint32_t* d_value_out, uint32_t n, void* d_scratch, size_t scratch_bytes,
                                    gms_stream_t stream);
 
+/* The other digit widths of the reference's multisplit sorts
+ * (multisplit_sort_{4,5,6,8}bit[_pairs], src/api/multisplit_sort.cuh:366-559,
+ * src/api/multisplit_sort_pairs.cuh:67-260), same schedules:
+ *   4: eight 4-bit passes;  5: six 5-bit passes then bits [30,32);
+ *   6: 4-bit, 4-bit, then four 6-bit passes;  7: as above;  8: four 8-bit passes.
+ * digit_bits outside 4..8 is GMS_ERROR_INVALID_VALUE. */
+gms_status gms_sort_scratch_bytes(uint32_t max_elements, int digit_bits, int key_value, size_t* bytes);
+gms_status gms_sort_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n, int digit_bits,
+                             void* d_scratch, size_t scratch_bytes, gms_stream_t stream);
+gms_status gms_sort_key_value(const uint32_t* d_key_in, uint32_t* d_key_out, const uint32_t* d_value_in,
+                              uint32_t* d_value_out, uint32_t n, int digit_bits, void* d_scratch,
+                              size_t scratch_bytes, gms_stream_t stream);
+
 /* ----------------------------------------------------------- compaction */
 /* Replaces compaction_allocate_key_only / _key_value
  * (src/kernels/compaction/multisplit2_compaction.cuh:491-517). */

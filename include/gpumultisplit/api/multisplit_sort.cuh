@@ -26,9 +26,9 @@ class ms_sort_context {
 
 namespace gms {
 namespace dropin {
-inline void sort_allocate(uint32_t n, ms_sort_context& c, int key_value) {
+inline void sort_allocate(uint32_t n, ms_sort_context& c, int key_value, int digit_bits = 7) {
   size_t bytes = 0;
-  gms_status st = gms_sort_7bit_scratch_bytes(n, key_value, &bytes);
+  gms_status st = gms_sort_scratch_bytes(n, digit_bits, key_value, &bytes);
   if (st == GMS_SUCCESS && cudaMalloc(&c.d_temp_storage, bytes) != cudaSuccess) st = GMS_ERROR_CUDA;
   last_status() = st;
   if (st != GMS_SUCCESS) return;
@@ -63,3 +63,28 @@ inline void multisplit_sort_7bit_pairs(uint32_t* d_key_in, uint32_t* d_key_out_m
   gms::last_status() = gms_sort_7bit_key_value(d_key_in, d_key_out_ms, d_value_in, d_value_out_ms, n_elements,
                                                context.d_temp_storage, context.temp_storage_bytes, 0);
 }
+
+// The other digit widths (src/api/multisplit_sort.cuh:118-559, src/api/multisplit_sort_pairs.cuh:67-260).
+#define GMS_DROPIN_SORT(BITS)                                                                                     \
+  inline void multisplit_sort_##BITS##bit_allocate(uint32_t n_elements, ms_sort_context& context) {               \
+    gms::dropin::sort_allocate(n_elements, context, 0, BITS);                                                     \
+  }                                                                                                               \
+  inline void multisplit_sort_##BITS##bit_allocate_pairs(uint32_t n_elements, ms_sort_context& context) {         \
+    gms::dropin::sort_allocate(n_elements, context, 1, BITS);                                                     \
+  }                                                                                                               \
+  inline void multisplit_sort_##BITS##bit(uint32_t* d_key_in, uint32_t* d_key_out_ms, uint32_t n_elements,        \
+                                          ms_sort_context& context) {                                             \
+    gms::last_status() = gms_sort_key_only(d_key_in, d_key_out_ms, n_elements, BITS, context.d_temp_storage,      \
+                                           context.temp_storage_bytes, 0);                                        \
+  }                                                                                                               \
+  inline void multisplit_sort_##BITS##bit_pairs(uint32_t* d_key_in, uint32_t* d_key_out_ms, uint32_t* d_value_in, \
+                                                uint32_t* d_value_out_ms, uint32_t n_elements,                    \
+                                                ms_sort_context& context) {                                       \
+    gms::last_status() = gms_sort_key_value(d_key_in, d_key_out_ms, d_value_in, d_value_out_ms, n_elements, BITS, \
+                                            context.d_temp_storage, context.temp_storage_bytes, 0);               \
+  }
+GMS_DROPIN_SORT(4)
+GMS_DROPIN_SORT(5)
+GMS_DROPIN_SORT(6)
+GMS_DROPIN_SORT(8)
+#undef GMS_DROPIN_SORT

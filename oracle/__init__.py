@@ -153,17 +153,24 @@ def histogram(keys, d: Desc) -> np.ndarray:
     return hist
 
 
-def sort_7bit(keys, values=None):
+def sort(keys, values=None, digit_bits: int = 7):
+    """Multisplit radix sort with the reference's schedule for `digit_bits` (4..8)."""
     keys = _u32(keys)
     n = keys.size
     kout, tk = np.empty(n, np.uint32), np.empty(n, np.uint32)
-    if values is None:
-        lib().oracle_sort_7bit(_p(keys), _p(kout), None, None, ctypes.c_uint32(n), _p(tk), None)
-        return kout, None
-    values = _u32(values)
-    vout, tv = np.empty(n, np.uint32), np.empty(n, np.uint32)
-    lib().oracle_sort_7bit(_p(keys), _p(kout), _p(values), _p(vout), ctypes.c_uint32(n), _p(tk), _p(tv))
+    vout = tv = None
+    if values is not None:
+        values = _u32(values)
+        vout, tv = np.empty(n, np.uint32), np.empty(n, np.uint32)
+    rc = lib().oracle_sort(_p(keys), _p(kout), _p(values), _p(vout), ctypes.c_uint32(n), _p(tk), _p(tv),
+                           ctypes.c_int(digit_bits))
+    if rc != 0:
+        raise ValueError(f"unknown digit width {digit_bits}")
     return kout, vout
+
+
+def sort_7bit(keys, values=None):
+    return sort(keys, values, 7)
 
 
 def compaction(keys, d: Desc, values=None):
@@ -214,7 +221,8 @@ def ref_multisplit_functor(keys, kind: int, num_buckets: int, param: int = 0, va
     return kout, vout
 
 
-def ref_sort_7bit(keys, values=None):
+def ref_sort(keys, values=None, digit_bits: int = 7):
+    """The reference's digit schedule for `digit_bits` run on the reference's CPU multisplit."""
     keys = _u32(keys)
     n = keys.size
     kout, tk = np.empty(n, np.uint32), np.empty(n, np.uint32)
@@ -222,5 +230,10 @@ def ref_sort_7bit(keys, values=None):
     if values is not None:
         values = _u32(values)
         vout, tv = np.empty(n, np.uint32), np.empty(n, np.uint32)
-    ref().ref_sort_7bit(_p(keys), _p(kout), _p(values), _p(vout), ctypes.c_uint32(n), _p(tk), _p(tv))
+    ref().ref_sort(_p(keys), _p(kout), _p(values), _p(vout), ctypes.c_uint32(n), _p(tk), _p(tv),
+                   ctypes.c_int(digit_bits))
     return kout, vout
+
+
+def ref_sort_7bit(keys, values=None):
+    return ref_sort(keys, values, 7)

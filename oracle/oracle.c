@@ -118,28 +118,45 @@ void oracle_histogram(const uint32_t* kin, uint32_t n, const oracle_desc* d, int
   for (uint32_t i = 0; i < n; ++i) hist[oracle_bucket(d, kin[i])]++;
 }
 
-/* 7-bit multisplit radix sort: a 4-bit pass then four 7-bit passes, each a
- * stable multisplit on a bit field (src/api/multisplit_sort.cuh:320-364,
- * src/api/multisplit_sort_pairs.cuh:21-65).  tmp_k/tmp_v hold n entries. */
-void oracle_sort_7bit(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
-                      uint32_t* tmp_k, uint32_t* tmp_v) {
-  static const uint32_t shifts[5] = {0, 4, 11, 18, 25};
-  static const uint32_t buckets[5] = {16, 128, 128, 128, 128};
+/* Multisplit radix sorts: stable multisplits on successive bit fields, least
+ * significant first, with the reference's digit schedules
+ * (src/api/multisplit_sort.cuh:320-559, src/api/multisplit_sort_pairs.cuh:21-260):
+ *   4: eight 4-bit digits; 5: six 5-bit digits then bits [30,32);
+ *   6: 4, 4, then four 6-bit digits; 7: 4 then four 7-bit digits; 8: four 8-bit.
+ * tmp_k/tmp_v hold n entries; returns 0, or -1 for an unknown width. */
+int oracle_sort(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                uint32_t* tmp_k, uint32_t* tmp_v, int digit_bits) {
+  static const uint32_t shifts[9][8] = {{0}, {0}, {0}, {0}, {0, 4, 8, 12, 16, 20, 24, 28},
+                                        {0, 5, 10, 15, 20, 25, 30}, {0, 4, 8, 14, 20, 26},
+                                        {0, 4, 11, 18, 25}, {0, 8, 16, 24}};
+  static const uint32_t buckets[9][8] = {{0}, {0}, {0}, {0}, {16, 16, 16, 16, 16, 16, 16, 16},
+                                         {32, 32, 32, 32, 32, 32, 4}, {16, 16, 64, 64, 64, 64},
+                                         {16, 128, 128, 128, 128}, {256, 256, 256, 256}};
+  static const int passes[9] = {0, 0, 0, 0, 8, 7, 6, 5, 4};
+  if (digit_bits < 4 || digit_bits > 8) return -1;
   const uint32_t* src_k = kin;
   const uint32_t* src_v = vin;
-  for (int p = 0; p < 5; ++p) {
-    /* passes 0, 2, 4 write the output buffer; 1, 3 the temporary one */
-    uint32_t* dk = (p % 2 == 0) ? kout : tmp_k;
-    uint32_t* dv = (p % 2 == 0) ? vout : tmp_v;
+  const int P = passes[digit_bits];
+  for (int p = 0; p < P; ++p) {
+    /* the last pass writes the output buffer, earlier ones alternate */
+    const int to_out = ((P - 1 - p) % 2) == 0;
+    uint32_t* dk = to_out ? kout : tmp_k;
+    uint32_t* dv = to_out ? vout : tmp_v;
     oracle_desc d;
     memset(&d, 0, sizeof(d));
     d.kind = ORACLE_BITS;
-    d.num_buckets = buckets[p];
-    d.shift = shifts[p];
+    d.num_buckets = buckets[digit_bits][p];
+    d.shift = shifts[digit_bits][p];
     multisplit(src_k, dk, vin ? src_v : NULL, vin ? dv : NULL, n, &d, NULL);
     src_k = dk;
     src_v = dv;
   }
+  return 0;
+}
+
+void oracle_sort_7bit(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                      uint32_t* tmp_k, uint32_t* tmp_v) {
+  oracle_sort(kin, kout, vin, vout, n, tmp_k, tmp_v, 7);
 }
 
 /* Two-bucket stable multisplit; returns the bucket-0 count

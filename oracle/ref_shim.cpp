@@ -14,6 +14,7 @@
 #include <functional>
 #include <iostream>
 #include <string>
+#include <vector>
 
 // The reference header names cudaMemcpy in a debug printer that is never
 // instantiated here; the CUDA runtime header only provides the declarations.
@@ -100,15 +101,33 @@ void ref_multisplit_functor(const uint32_t* kin, uint32_t* kout, const uint32_t*
   }
 }
 
-// The reference's 7-bit sort schedule (src/api/multisplit_sort.cuh:333-363)
-// driven by the reference's CPU multisplit: 4-bit pass, then 7-bit passes at 4, 11, 18, 25.
-void ref_sort_7bit(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
-                   uint32_t* tmp_k, uint32_t* tmp_v) {
-  run(kin, kout, vin, vout, n, BitField{0, 0x0F}, 16);
-  run(kout, tmp_k, vin ? vout : nullptr, tmp_v, n, BitField{4, 0x7F}, 128);
-  run(tmp_k, kout, vin ? tmp_v : nullptr, vout, n, BitField{11, 0x7F}, 128);
-  run(kout, tmp_k, vin ? vout : nullptr, tmp_v, n, BitField{18, 0x7F}, 128);
-  run(tmp_k, kout, vin ? tmp_v : nullptr, vout, n, BitField{25, 0x7F}, 128);
+// The reference's sort digit schedules (src/api/multisplit_sort.cuh:320-559)
+// driven by the reference's CPU multisplit; the last pass lands in kout.
+void ref_sort(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n, uint32_t* tmp_k,
+              uint32_t* tmp_v, int digit_bits) {
+  struct Pass {
+    uint32_t shift, mask;
+  };
+  std::vector<Pass> s;
+  switch (digit_bits) {
+    case 4: for (uint32_t x = 0; x < 32; x += 4) s.push_back({x, 0x0F}); break;
+    case 5: for (uint32_t x = 0; x < 30; x += 5) s.push_back({x, 0x1F}); s.push_back({30, 0x03}); break;
+    case 6: s = {{0, 0x0F}, {4, 0x0F}, {8, 0x3F}, {14, 0x3F}, {20, 0x3F}, {26, 0x3F}}; break;
+    case 7: s = {{0, 0x0F}, {4, 0x7F}, {11, 0x7F}, {18, 0x7F}, {25, 0x7F}}; break;
+    case 8: s = {{0, 0xFF}, {8, 0xFF}, {16, 0xFF}, {24, 0xFF}}; break;
+    default: return;
+  }
+  const uint32_t* sk = kin;
+  const uint32_t* sv = vin;
+  const int P = int(s.size());
+  for (int p = 0; p < P; ++p) {
+    const bool to_out = ((P - 1 - p) % 2) == 0;
+    uint32_t* dk = to_out ? kout : tmp_k;
+    uint32_t* dv = to_out ? vout : tmp_v;
+    run(sk, dk, vin ? sv : nullptr, dv, n, BitField{s[p].shift, s[p].mask}, s[p].mask + 1);
+    sk = dk;
+    sv = dv;
+  }
 }
 
 }  // extern "C"

@@ -118,7 +118,18 @@ static void test_multisplit(const char* name, uint32_t n, uint32_t B, F f) {
   printf("multisplit %-28s n=%u B=%u\n", name, n, B);
 }
 
-static void test_sort(uint32_t n, bool and4) {
+struct SortFns {
+  int bits;
+  void (*allocate)(uint32_t, ms_sort_context&);
+  void (*allocate_pairs)(uint32_t, ms_sort_context&);
+  void (*keys)(uint32_t*, uint32_t*, uint32_t, ms_sort_context&);
+  void (*pairs)(uint32_t*, uint32_t*, uint32_t*, uint32_t*, uint32_t, ms_sort_context&);
+};
+#define SORT_FNS(B) \
+  SortFns { B, multisplit_sort_##B##bit_allocate, multisplit_sort_##B##bit_allocate_pairs, multisplit_sort_##B##bit, \
+            multisplit_sort_##B##bit_pairs }
+
+static void test_sort(uint32_t n, bool and4, SortFns fns = SORT_FNS(7)) {
   std::vector<uint32_t> k(n), v(n);
   for (uint32_t i = 0; i < n; ++i) {
     k[i] = and4 ? (next_u32() & next_u32() & next_u32() & next_u32()) : next_u32();
@@ -133,21 +144,21 @@ static void test_sort(uint32_t n, bool and4) {
   cudaMemcpy(d.k, k.data(), 4 * n, cudaMemcpyHostToDevice);
   cudaMemcpy(d.v, v.data(), 4 * n, cudaMemcpyHostToDevice);
   ms_sort_context ctx;
-  multisplit_sort_7bit_allocate_pairs(n, ctx);
-  multisplit_sort_7bit_pairs(d.k, d.ko, d.v, d.vo, n, ctx);  // reference order: kin, kout, vin, vout
+  fns.allocate_pairs(n, ctx);
+  fns.pairs(d.k, d.ko, d.v, d.vo, n, ctx);  // reference order: kin, kout, vin, vout
   cudaDeviceSynchronize();
   CHECK(multisplit_last_error() == GMS_SUCCESS, "sort pairs");
   CHECK(download(d.ko, n) == rk, "sort pairs keys");
   CHECK(download(d.vo, n) == idx, "sort pairs values (stable)");
   multisplit_sort_release_memory(ctx);
   ms_sort_context ctx2;
-  multisplit_sort_7bit_allocate(n, ctx2);
-  multisplit_sort_7bit(d.k, d.ko, n, ctx2);
+  fns.allocate(n, ctx2);
+  fns.keys(d.k, d.ko, n, ctx2);
   cudaDeviceSynchronize();
   CHECK(download(d.ko, n) == rk, "sort keys");
   CHECK(download(d.k, n) == k, "sort leaves its input untouched");
   multisplit_sort_release_memory(ctx2);
-  printf("sort 7-bit n=%u %s\n", n, and4 ? "and4" : "uniform");
+  printf("sort %d-bit n=%u %s\n", fns.bits, n, and4 ? "and4" : "uniform");
 }
 
 template <class F>
@@ -208,6 +219,10 @@ int main() {
   test_multisplit("user hash_bucket, n=1", 1, 64, hash_bucket());
   test_sort(100003, false);
   test_sort(65536, true);
+  test_sort(50001, false, SORT_FNS(4));
+  test_sort(50002, true, SORT_FNS(5));
+  test_sort(50003, false, SORT_FNS(6));
+  test_sort(50004, false, SORT_FNS(8));
   test_compaction("test_bucket<1> (key & 1)", 100001, test_bucket<1, uint32_t>());
   test_compaction("gms::mask_bucket{1}", 4096, gms::mask_bucket{1});
   test_histogram("gms::delta_bucket", 1 << 20, 256, gms::delta_bucket{256});

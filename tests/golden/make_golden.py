@@ -10,8 +10,8 @@ bucket offsets for the rest.  Outputs come from cpu_multisplit_general /
 cpu_multisplit_pairs_general (src/cpu_functions.h:155-288) compiled from the
 reference sources, driven either by reference-style functors (key*B>>32 as top
 bits, delta_func's key/delta, ms_bucket_sort's bit field) or by the oracle's
-bucket function (range, mask, even-float identifiers).  The 7-bit sort cases
-run the reference's digit schedule (src/api/multisplit_sort.cuh:333-363) on
+bucket function (range, mask, even-float identifiers).  The sort cases
+run the reference's digit schedules (src/api/multisplit_sort.cuh:320-559) on
 that same reference CPU multisplit and are checked against numpy's stable sort.
 """
 from __future__ import annotations
@@ -173,6 +173,17 @@ def main() -> None:
         if with_values:
             assert np.array_equal(vo, np.argsort(keys, kind="stable").astype(np.uint32))
         case = {"name": name, "op": "sort7", "dist": dist, "n": n, "seed": seed, "values": with_values}
+        cases.append(record(case, keys, ko, vo, None))
+
+    # The other digit widths (src/api/multisplit_sort.cuh:366-559), same check.
+    for bits, n, seed in ((4, 50001, 34), (5, 50002, 35), (6, 50003, 36), (8, 50004, 37)):
+        keys = gen_keys("uniform", n, seed)
+        vals = np.arange(n, dtype=np.uint32)
+        ko, vo = oracle.ref_sort(keys, vals, bits)
+        assert np.array_equal(ko, np.sort(keys))
+        assert np.array_equal(vo, np.argsort(keys, kind="stable").astype(np.uint32))
+        case = {"name": f"sort{bits}_pairs_uniform", "op": "sort", "digit_bits": bits, "dist": "uniform", "n": n,
+                "seed": seed, "values": True}
         cases.append(record(case, keys, ko, vo, None))
 
     OUT.write_text(json.dumps({"generator": "tests/golden/make_golden.py", "cases": cases}, indent=1) + "\n")

@@ -1,4 +1,4 @@
-"""GPU parity of the 7-bit multisplit radix sort, the two-bucket compaction and
+"""GPU parity of the multisplit radix sorts (4- to 8-bit digits), the two-bucket compaction and
 the histogram entry points against the CPU oracle (bit-exact)."""
 import hashlib
 
@@ -13,19 +13,20 @@ from gpu_util import KIND_NAMES, host, identifiers, to_dev
 pytestmark = pytest.mark.gpu
 
 
-def sort_gpu(keys, values=None, misalign=0):
+def sort_gpu(keys, values=None, misalign=0, bits=7):
     n = keys.size
     dk, ok = to_dev(keys, misalign), to_dev(np.zeros(n, np.uint32), misalign)
     ctx = gms.ms_sort_context()
+    fn = f"multisplit_sort_{bits}bit"
     if values is None:
-        gms.multisplit_sort_7bit_allocate(n, ctx)
-        gms.multisplit_sort_7bit(dk, ok, n, ctx)
+        getattr(gms, fn + "_allocate")(n, ctx)
+        getattr(gms, fn)(dk, ok, n, ctx)
         torch.cuda.synchronize()
         out = host(ok), None
     else:
         dv, ov = to_dev(values, misalign), to_dev(np.zeros(n, np.uint32), misalign)
-        gms.multisplit_sort_7bit_allocate_pairs(n, ctx)
-        gms.multisplit_sort_7bit_pairs(dk, ok, dv, ov, n, ctx)
+        getattr(gms, fn + "_allocate_pairs")(n, ctx)
+        getattr(gms, fn + "_pairs")(dk, ok, dv, ov, n, ctx)
         torch.cuda.synchronize()
         out = host(ok), host(ov)
     # the input is not modified (src/api/multisplit_sort.cuh:340-363 never writes d_key_in)
@@ -55,15 +56,30 @@ def test_sort7_misaligned(gms_lib):
     np.testing.assert_array_equal(gv, np.argsort(keys, kind="stable"))
 
 
+@pytest.mark.parametrize("bits", [4, 5, 6, 8])
+@pytest.mark.parametrize("n", [0, 1, 4097, 100003, 1 << 20])
+def test_sort_other_widths(gms_lib, oracle_mod, bits, n):
+    """multisplit_sort_{4,5,6,8}bit[_pairs] (src/api/multisplit_sort.cuh:366-559,
+    src/api/multisplit_sort_pairs.cuh:67-260)."""
+    keys = datagen.as_u32(datagen.uniform_u32(n, 300 + bits + n))
+    vals = np.arange(n, dtype=np.uint32)
+    gk, _ = sort_gpu(keys, bits=bits)
+    np.testing.assert_array_equal(gk, np.sort(keys))
+    gk, gv = sort_gpu(keys, vals, misalign=bits & 1, bits=bits)
+    rk, rv = oracle_mod.sort(keys, vals, bits)
+    np.testing.assert_array_equal(gk, rk)
+    np.testing.assert_array_equal(gv, rv)
+
+
 def test_sort7_golden(gms_lib, golden):
     from test_oracle_golden import gen_keys, sha
 
     for case in golden:
-        if case["op"] != "sort7":
+        if case["op"] not in ("sort7", "sort"):
             continue
         keys = gen_keys(case)
         vals = np.arange(case["n"], dtype=np.uint32) if case["values"] else None
-        gk, gv = sort_gpu(keys, vals)
+        gk, gv = sort_gpu(keys, vals, bits=case.get("digit_bits", 7))
         assert sha(gk) == case["keys_out_sha256"], case["name"]
         if vals is not None:
             assert sha(gv) == case["values_out_sha256"], case["name"]

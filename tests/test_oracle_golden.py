@@ -55,6 +55,8 @@ def test_oracle_matches_golden(golden, oracle_mod):
             assert n0 == case["num_bucket0"], case["name"]
         elif case["op"] == "sort7":
             ko, vo = o.sort_7bit(keys, vals)
+        elif case["op"] == "sort":
+            ko, vo = o.sort(keys, vals, case["digit_bits"])
         else:
             raise AssertionError(case["op"])
         assert sha(ko) == case["keys_out_sha256"], case["name"]
@@ -108,13 +110,16 @@ def test_multithreaded_port_matches(oracle_mod):
         assert np.array_equal(ko, mk) and np.array_equal(vo, mv)
 
 
-def test_sort_oracle_is_stable_sort(oracle_mod):
+@pytest.mark.parametrize("bits", [4, 5, 6, 7, 8])
+def test_sort_oracle_is_stable_sort(oracle_mod, bits):
     o = oracle_mod
     keys = datagen.as_u32(datagen.and4_u32(50000, 9))
     vals = np.arange(keys.size, dtype=np.uint32)
-    ko, vo = o.sort_7bit(keys, vals)
+    ko, vo = o.sort(keys, vals, bits)
     assert np.array_equal(ko, np.sort(keys))
     assert np.array_equal(vo, np.argsort(keys, kind="stable"))
+    with pytest.raises(ValueError):
+        o.sort(keys, vals, 3)
 
 
 @pytest.mark.skipif("not __import__('oracle').ref_available()", reason="reference CPU library not built here")
