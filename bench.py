@@ -217,7 +217,14 @@ def run_batched(dev, reps: int = 3):
         for ki, vi, ko, vo, n, B, ident in plain:
             gms.multisplit_key_value(ki, vi, ko, vo, n, ctxs[B], ident)
 
+    # Tile shapes per (B, size class) for this device, then the plan from the tuned table.
+    t0 = time.perf_counter()
+    gms.autotune(buckets=(2, 8, 32, 256), key_value=(True,), keys_per_trial=1 << 24, reps=3)
+    autotune_s = time.perf_counter() - t0
+    table = gms.tuning_table()
+    chosen = {f"B{B}": [gms.tile_variant_shape(table[(B, True, c)])[2] for c in range(8)] for B in (2, 8, 32, 256)}
     plan = gms.BatchedMultisplit(segs)
+    plan_fixed = gms.BatchedMultisplit(segs, variant=0)
 
     def timed(fn, count):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -238,6 +245,10 @@ def run_batched(dev, reps: int = 3):
     graph_ms, _ = timed(lambda: plan.run(use_graph=True), max(reps, 5))
     nograph_ms, _ = timed(lambda: plan.run(use_graph=False), max(reps, 5))
     identical = bool(torch.equal(kout, kref) and torch.equal(vout, vref))
+    plan_fixed.run(use_graph=True)
+    fixed_ms, _ = timed(lambda: plan_fixed.run(use_graph=True), max(reps, 5))
+    identical = identical and bool(torch.equal(kout, kref) and torch.equal(vout, vref))
+    plan_fixed.close()
     peak, _ = hbm_peak()
     res = {
         "workload": f"{len(sizes)} key-value segments, sizes log-uniform in [1024, 4194304] (seed 7), "
@@ -246,6 +257,9 @@ def run_batched(dev, reps: int = 3):
         "batched_graph_ms": graph_ms,
         "batched_graph_gkeys": total / (graph_ms * 1e-3) / 1e9,
         "batched_nograph_ms": nograph_ms,
+        "batched_one_tile_shape_ms": fixed_ms,
+        "autotune_s": autotune_s,
+        "tuned_tile_keys_by_size_class": chosen,
         "plain_per_call_ms": plain_ms,
         "plain_per_call_gkeys": total / (plain_ms * 1e-3) / 1e9,
         "plain_host_wall_ms": plain_wall,

@@ -44,5 +44,13 @@ from .api import (  # noqa: F401
     multisplit_sort_6bit, multisplit_sort_6bit_allocate, multisplit_sort_6bit_allocate_pairs, multisplit_sort_6bit_pairs,
     multisplit_sort_8bit, multisplit_sort_8bit_allocate, multisplit_sort_8bit_allocate_pairs, multisplit_sort_8bit_pairs,
 )
-from .batched import BatchedMultisplit, Segment  # noqa: F401
+from .batched import (  # noqa: F401
+    BatchedMultisplit,
+    Segment,
+    autotune,
+    reset_tuning,
+    set_tuning,
+    tile_variant_shape,
+    tuning_table,
+)
 from .serving import Result, Server  # noqa: F401

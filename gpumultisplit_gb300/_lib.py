@@ -87,6 +87,12 @@ _PROTOS = {
     "gms_batch_run": [_P, _P, _SZ, _I32, _P],
     "gms_batch_launch_count": [_P, _PU32],
     "gms_batch_destroy": [_P],
+    "gms_batch_create_with_variant": [_P, _U32, _I32, _P],
+    "gms_tile_variant_shape": [_I32, _PU32, _PU32, _PU32],
+    "gms_tuning_get": [_U32, _I32, _I32, ctypes.POINTER(ctypes.c_int)],
+    "gms_tuning_set": [_U32, _I32, _I32, _I32],
+    "gms_tuning_reset": [],
+    "gms_autotune": [_U32, _U32, _U32, _I32, ctypes.POINTER(ctypes.c_float), _P],
     "gms_server_create": [_P, _SZ, _P],
     "gms_server_submit": [_P, _P, _P],
     "gms_server_poll": [_P, ctypes.c_uint64, _P],

@@ -34,8 +34,28 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build gpumultisplit_gb300")
 
 
+# inst_batch.cu is compiled once per (identifier kind, tile variant); the
+# counts match NUM_KINDS in gms_device.cuh and kNumTileVariants in ms_host.h.
+BATCH_INST = "inst_batch.cu"
+NUM_KINDS = 6
+NUM_TILE_VARIANTS = 4
+
+
 def _sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu"))
+
+
+def _units() -> list[tuple[Path, str, list[str]]]:
+    """(source, object stem, extra flags) of every translation unit."""
+    units = []
+    for s in _sources():
+        if s.name == BATCH_INST:
+            for k in range(NUM_KINDS):
+                for v in range(NUM_TILE_VARIANTS):
+                    units.append((s, f"{s.stem}_k{k}_v{v}", [f"-DGMS_INST_KIND={k}", f"-DGMS_INST_VARIANT={v}"]))
+        else:
+            units.append((s, s.stem, []))
+    return units
 
 
 def _deps() -> list[Path]:
@@ -67,11 +87,14 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     obj_dir = LIB_DIR / "obj"
     obj_dir.mkdir(parents=True, exist_ok=True)
     flags = ARCH_FLAGS + NVCC_FLAGS + list(extra_flags or [])
-    srcs = _sources()
-    objs = [obj_dir / (s.stem + ".o") for s in srcs]
-    jobs = max(1, min(len(srcs), os.cpu_count() or 4))
+    units = _units()
+    # Largest units first so the parallel build ends sooner.
+    units.sort(key=lambda u: (not u[1].startswith("inst_"), u[1].startswith(BATCH_INST[:-3])))
+    objs = [obj_dir / (stem + ".o") for _, stem, _ in units]
+    jobs = max(1, min(len(units), os.cpu_count() or 4))
     with ThreadPoolExecutor(max_workers=jobs) as ex:
-        futs = [ex.submit(_run, [nvcc, *flags, "-c", str(s), "-o", str(o)], verbose) for s, o in zip(srcs, objs)]
+        futs = [ex.submit(_run, [nvcc, *flags, *extra, "-c", str(s), "-o", str(o)], verbose)
+                for (s, _, extra), o in zip(units, objs)]
         for f in futs:
             f.result()
     tmp = LIB_DIR / (LIB_PATH.name + ".tmp")

@@ -19,6 +19,7 @@ struct BatchClass {
   int kind = 0;
   int logb = 1;
   bool kv = false;
+  int variant = 0;           // tile shape (kTileVariants)
   std::vector<uint2> tiles;  // (segment, tile)
   size_t map_off = 0;        // byte offset of this class's map in scratch
 };
@@ -64,17 +65,17 @@ bool log2_buckets(uint32_t b, int* logb) {
   return true;
 }
 
-cudaError_t dispatch_class(int kind, const BatchClassLaunch& c, int stage) {
-  switch (kind) {
-    case KIND_DELTA: return run_batch_class<KIND_DELTA>(c, stage);
-    case KIND_DIV: return run_batch_class<KIND_DIV>(c, stage);
-    case KIND_BITS: return run_batch_class<KIND_BITS>(c, stage);
-    case KIND_RANGE: return run_batch_class<KIND_RANGE>(c, stage);
-    case KIND_MASK: return run_batch_class<KIND_MASK>(c, stage);
-    case KIND_EVEN_FLOAT: return run_batch_class<KIND_EVEN_FLOAT>(c, stage);
+template <int KIND>
+cudaError_t dispatch_variant(const BatchClassLaunch& c, int stage) {
+  switch (c.variant) {
+    case 0: return run_batch_class_v<KIND, 0>(c, stage);
+    case 1: return run_batch_class_v<KIND, 1>(c, stage);
+    case 2: return run_batch_class_v<KIND, 2>(c, stage);
+    case 3: return run_batch_class_v<KIND, 3>(c, stage);
     default: return cudaErrorInvalidValue;
   }
 }
+static_assert(kNumTileVariants == 4, "dispatch_variant covers every tile variant");
 
 // The launch sequence of one run: reset the error word, prescan every class,
 // scan every group (ticket and status words reset first), postscan every class.
@@ -102,9 +103,10 @@ cudaError_t launch_all(gms_batch_s* b, unsigned char* scratch, cudaStream_t s) {
     for (const BatchClass& c : b->classes) {
       L.logb = c.logb;
       L.kv = c.kv;
+      L.variant = c.variant;
       L.tile_map = reinterpret_cast<const uint2*>(scratch + c.map_off);
       L.class_tiles = uint32_t(c.tiles.size());
-      e = dispatch_class(c.kind, L, stage);
+      e = run_batch_class(c.kind, L, stage);
       if (e != cudaSuccess) return e;
     }
   }
@@ -112,16 +114,24 @@ cudaError_t launch_all(gms_batch_s* b, unsigned char* scratch, cudaStream_t s) {
 }
 
 }  // namespace
-}  // namespace gms
 
-using namespace gms;
+cudaError_t run_batch_class(int kind, const BatchClassLaunch& c, int stage) {
+  switch (kind) {
+    case KIND_DELTA: return dispatch_variant<KIND_DELTA>(c, stage);
+    case KIND_DIV: return dispatch_variant<KIND_DIV>(c, stage);
+    case KIND_BITS: return dispatch_variant<KIND_BITS>(c, stage);
+    case KIND_RANGE: return dispatch_variant<KIND_RANGE>(c, stage);
+    case KIND_MASK: return dispatch_variant<KIND_MASK>(c, stage);
+    case KIND_EVEN_FLOAT: return dispatch_variant<KIND_EVEN_FLOAT>(c, stage);
+    default: return cudaErrorInvalidValue;
+  }
+}
 
-extern "C" {
-
-gms_status gms_batch_create(const gms_segment* segments, uint32_t count, gms_batch_t* batch) {
-  if (batch == nullptr || (segments == nullptr && count > 0)) return GMS_ERROR_INVALID_VALUE;
+gms_status batch_create(const gms_segment* segments, uint32_t count, int variant, gms_batch_t* batch) {
+  if (batch == nullptr || (segments == nullptr && count > 0) || variant >= kNumTileVariants)
+    return GMS_ERROR_INVALID_VALUE;
   auto* b = new gms_batch_s();
-  std::map<std::tuple<int, int, bool>, size_t> class_index;
+  std::map<std::tuple<int, int, bool, int>, size_t> class_index;
   uint64_t matrix_total = 0, group_n = 0;
   ScanGroup group;
   for (uint32_t i = 0; i < count; ++i) {
@@ -152,7 +162,12 @@ gms_status gms_batch_create(const gms_segment* segments, uint32_t count, gms_bat
     d.bp.lower = sg.desc.lower;
     d.bp.inverse_delta = sg.desc.inverse_delta;
     d.bp.splitters = sg.desc.d_splitters;
-    const uint32_t tile = tile_keys(logb, kv);
+    const int v = variant >= 0 ? variant : tuned_variant(logb, kv, sg.n);
+    if (!variant_valid(v, logb)) {
+      delete b;
+      return GMS_ERROR_INVALID_VALUE;
+    }
+    const uint32_t tile = variant_tile_keys(v);
     d.num_tiles = uint32_t((uint64_t(sg.n) + tile - 1) / tile);
     const uint64_t entries = uint64_t(1u << logb) * d.num_tiles;
     // Start a new scan group when this segment would push the group's keys past 2^32 - 1.
@@ -172,7 +187,7 @@ gms_status gms_batch_create(const gms_segment* segments, uint32_t count, gms_bat
     }
     b->segs.push_back(d);
     if (d.num_tiles == 0) continue;
-    const auto key = std::make_tuple(kind, logb, kv);
+    const auto key = std::make_tuple(kind, logb, kv, v);
     auto it = class_index.find(key);
     if (it == class_index.end()) {
       it = class_index.emplace(key, b->classes.size()).first;
@@ -180,6 +195,7 @@ gms_status gms_batch_create(const gms_segment* segments, uint32_t count, gms_bat
       c.kind = kind;
       c.logb = logb;
       c.kv = kv;
+      c.variant = v;
       b->classes.push_back(c);
     }
     auto& tiles = b->classes[it->second].tiles;
@@ -204,6 +220,22 @@ gms_status gms_batch_create(const gms_segment* segments, uint32_t count, gms_bat
   b->bytes = align_up(off + size_t(b->max_chunks) * 8, 256);
   *batch = b;
   return GMS_SUCCESS;
+}
+
+}  // namespace gms
+
+using namespace gms;
+
+extern "C" {
+
+gms_status gms_batch_create(const gms_segment* segments, uint32_t count, gms_batch_t* batch) {
+  return batch_create(segments, count, -1, batch);
+}
+
+gms_status gms_batch_create_with_variant(const gms_segment* segments, uint32_t count, int variant,
+                                         gms_batch_t* batch) {
+  if (variant < 0) return GMS_ERROR_INVALID_VALUE;
+  return batch_create(segments, count, variant, batch);
 }
 
 gms_status gms_batch_scratch_bytes(gms_batch_t batch, size_t* bytes) {

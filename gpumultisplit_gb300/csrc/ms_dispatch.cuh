@@ -118,45 +118,50 @@ cudaError_t run_multisplit(const MsCall& c, int stages) {
   return c.kv ? run_multisplit_kv<KIND, true>(c, stages) : run_multisplit_kv<KIND, false>(c, stages);
 }
 
-template <int KIND, int LOGB, bool KV>
+template <int KIND, int LOGB, bool KV, int V>
 cudaError_t run_batch_class_t(const BatchClassLaunch& c, int stage) {
-  using S = TileShape<LOGB, KV>;
-  using C = TileCfg<LOGB, S::WARPS, S::IPT, KV>;
-  if (c.class_tiles == 0) return cudaSuccess;
-  if (stage == STAGE_PRESCAN) {
-    static std::atomic<int> per_sm{0};
-    auto kern = batch_prescan_kernel<C, KIND>;
-    const uint32_t grid = persistent_grid(kern, C::THREADS, c.class_tiles, per_sm);
-    kern<<<grid, C::THREADS, 0, c.stream>>>(c.segs, c.tile_map, c.class_tiles, c.matrix);
+  constexpr int WARPS = kTileVariants[V].warps;
+  constexpr int IPT = kTileVariants[V].ipt;
+  if constexpr (WARPS * 32 < (1 << LOGB)) {
+    return cudaErrorInvalidValue;  // the shape has fewer threads than buckets
+  } else {
+    using C = TileCfg<LOGB, WARPS, IPT, KV>;
+    if (c.class_tiles == 0) return cudaSuccess;
+    if (stage == STAGE_PRESCAN) {
+      static std::atomic<int> per_sm{0};
+      auto kern = batch_prescan_kernel<C, KIND>;
+      const uint32_t grid = persistent_grid(kern, C::THREADS, c.class_tiles, per_sm);
+      kern<<<grid, C::THREADS, 0, c.stream>>>(c.segs, c.tile_map, c.class_tiles, c.matrix);
+      return cudaGetLastError();
+    }
+    static std::atomic<uint64_t> smem_done{0};
+    auto kern = batch_postscan_kernel<C, KIND>;
+    constexpr size_t smem = PostLayout<C, DescPolicy<KIND, LOGB>>::BYTES;
+    cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
+    if (e != cudaSuccess) return e;
+    kern<<<c.class_tiles, C::THREADS, smem, c.stream>>>(c.segs, c.tile_map, c.matrix, c.hdr);
     return cudaGetLastError();
   }
-  static std::atomic<uint64_t> smem_done{0};
-  auto kern = batch_postscan_kernel<C, KIND>;
-  constexpr size_t smem = PostLayout<C, DescPolicy<KIND, LOGB>>::BYTES;
-  cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
-  if (e != cudaSuccess) return e;
-  kern<<<c.class_tiles, C::THREADS, smem, c.stream>>>(c.segs, c.tile_map, c.matrix, c.hdr);
-  return cudaGetLastError();
 }
 
-template <int KIND, bool KV>
+template <int KIND, bool KV, int V>
 cudaError_t run_batch_class_kv(const BatchClassLaunch& c, int stage) {
   switch (c.logb) {
-    case 1: return run_batch_class_t<KIND, 1, KV>(c, stage);
-    case 2: return run_batch_class_t<KIND, 2, KV>(c, stage);
-    case 3: return run_batch_class_t<KIND, 3, KV>(c, stage);
-    case 4: return run_batch_class_t<KIND, 4, KV>(c, stage);
-    case 5: return run_batch_class_t<KIND, 5, KV>(c, stage);
-    case 6: return run_batch_class_t<KIND, 6, KV>(c, stage);
-    case 7: return run_batch_class_t<KIND, 7, KV>(c, stage);
-    case 8: return run_batch_class_t<KIND, 8, KV>(c, stage);
+    case 1: return run_batch_class_t<KIND, 1, KV, V>(c, stage);
+    case 2: return run_batch_class_t<KIND, 2, KV, V>(c, stage);
+    case 3: return run_batch_class_t<KIND, 3, KV, V>(c, stage);
+    case 4: return run_batch_class_t<KIND, 4, KV, V>(c, stage);
+    case 5: return run_batch_class_t<KIND, 5, KV, V>(c, stage);
+    case 6: return run_batch_class_t<KIND, 6, KV, V>(c, stage);
+    case 7: return run_batch_class_t<KIND, 7, KV, V>(c, stage);
+    case 8: return run_batch_class_t<KIND, 8, KV, V>(c, stage);
     default: return cudaErrorInvalidValue;
   }
 }
 
-template <int KIND>
-cudaError_t run_batch_class(const BatchClassLaunch& c, int stage) {
-  return c.kv ? run_batch_class_kv<KIND, true>(c, stage) : run_batch_class_kv<KIND, false>(c, stage);
+template <int KIND, int V>
+cudaError_t run_batch_class_v(const BatchClassLaunch& c, int stage) {
+  return c.kv ? run_batch_class_kv<KIND, true, V>(c, stage) : run_batch_class_kv<KIND, false, V>(c, stage);
 }
 
 template <int KIND, int LOGB>
@@ -190,6 +195,7 @@ cudaError_t run_histogram(const uint32_t* keys, uint32_t n, int logb, const Buck
 
 #define GMS_INSTANTIATE_KIND(K)                                                                        \
   template cudaError_t gms::run_multisplit<K>(const gms::MsCall&, int);                                \
-  template cudaError_t gms::run_batch_class<K>(const gms::BatchClassLaunch&, int);                     \
   template cudaError_t gms::run_histogram<K>(const uint32_t*, uint32_t, int, const gms::BucketParams&, \
                                              int32_t*, cudaStream_t);
+
+#define GMS_INSTANTIATE_BATCH(K, V) template cudaError_t gms::run_batch_class_v<K, V>(const gms::BatchClassLaunch&, int);

@@ -24,6 +24,32 @@ struct TileShape {
 
 uint32_t tile_keys(int logb, bool kv);
 
+// Tile shapes the batched form can run, chosen per (bucket count, key/value,
+// segment size class) by the tuning table (tuning.cu).  Variant 0 is the plain
+// path's shape.  A shape needs at least one thread per bucket (tile scan).
+struct TileVariantShape {
+  int warps;
+  int ipt;  // keys per thread
+};
+constexpr int kNumTileVariants = 4;
+constexpr TileVariantShape kTileVariants[kNumTileVariants] = {{8, 16}, {8, 8}, {8, 4}, {4, 16}};
+inline bool variant_valid(int v, int logb) {
+  return v >= 0 && v < kNumTileVariants && kTileVariants[v].warps * 32 >= (1 << logb);
+}
+inline uint32_t variant_tile_keys(int v) { return uint32_t(kTileVariants[v].warps) * 32u * kTileVariants[v].ipt; }
+
+// Segment size classes of the tuning table: 0 for n <= 2^10, c for
+// 2^(9+c) < n <= 2^(10+c), up to kNumSizeClasses - 1 for n > 2^16.
+constexpr int kNumSizeClasses = 8;
+inline int size_class(uint32_t n) {
+  int c = 0;
+  while (c < kNumSizeClasses - 1 && n > (1u << (10 + c))) ++c;
+  return c;
+}
+
+// Variant the batched form uses for a segment (the tuning table's entry).
+int tuned_variant(int logb, bool kv, uint32_t n);
+
 constexpr uint32_t kScanChunk = 4096;  // SCAN_CHUNK in scan_kernels.cuh
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -85,6 +111,7 @@ struct SegDesc;
 struct BatchClassLaunch {
   int logb = 1;
   bool kv = false;
+  int variant = 0;                  // tile shape (kTileVariants)
   const SegDesc* segs = nullptr;    // device
   const uint2* tile_map = nullptr;  // device, class_tiles entries of (segment, tile)
   uint32_t class_tiles = 0;
@@ -94,9 +121,17 @@ struct BatchClassLaunch {
 };
 
 // Launches the prescan (STAGE_PRESCAN) or postscan (STAGE_POSTSCAN) of one
-// batch class.  Defined per identifier kind in inst_*.cu.
-template <int KIND>
-cudaError_t run_batch_class(const BatchClassLaunch& c, int stage);
+// batch class with tile variant V.  Instantiated per (kind, variant) from
+// inst_batch.cu.
+template <int KIND, int V>
+cudaError_t run_batch_class_v(const BatchClassLaunch& c, int stage);
+
+// Dispatch on the class's kind and variant (batch.cu).
+cudaError_t run_batch_class(int kind, const BatchClassLaunch& c, int stage);
+
+// Creates a batch plan whose every class uses `variant` (>= 0), or the tuning
+// table's choice per segment (variant < 0).
+gms_status batch_create(const gms_segment* segments, uint32_t count, int variant, gms_batch_t* batch);
 
 int device_sm_count();
 

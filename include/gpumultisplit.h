@@ -222,6 +222,37 @@ gms_status gms_batch_run(gms_batch_t batch, void* d_scratch, size_t scratch_byte
 /* Number of kernel launches one run issues (inside the graph when use_graph != 0). */
 gms_status gms_batch_launch_count(gms_batch_t batch, uint32_t* launches);
 gms_status gms_batch_destroy(gms_batch_t batch);
+/* Builds a plan whose every segment runs tile variant `variant` instead of
+ * the tuning table's choice (for measurements and tests). */
+gms_status gms_batch_create_with_variant(const gms_segment* segments, uint32_t count, int variant,
+                                         gms_batch_t* batch);
+
+/* -------------------------------------------------------------- tuning */
+/* The batched form runs each segment with one of GMS_NUM_TILE_VARIANTS tile
+ * shapes (warps per block x keys per thread), picked from a process-wide
+ * table indexed by (log2 B, key/value, segment size class).  Size class c
+ * covers n <= 2^10 for c = 0, 2^(9+c) < n <= 2^(10+c) for 0 < c < 7, and
+ * n > 2^16 for c = 7.  A shape is valid for B only when it has at least B
+ * threads.  gms_batch_create reads the table, so a change applies to plans
+ * created afterwards. */
+#define GMS_NUM_TILE_VARIANTS 4
+#define GMS_NUM_SIZE_CLASSES 8
+gms_status gms_tile_variant_shape(int variant, uint32_t* warps, uint32_t* keys_per_thread, uint32_t* tile_keys);
+gms_status gms_tuning_get(uint32_t num_buckets, int key_value, int size_class, int* variant);
+gms_status gms_tuning_set(uint32_t num_buckets, int key_value, int size_class, int variant);
+/* Restores the built-in table (before any autotuning). */
+gms_status gms_tuning_reset(void);
+/* Autotuner: for every bucket count whose bit is set in bucket_mask (bit k =
+ * 2^k buckets, k = 1..8), every shape in key_value_mask (bit 0 key-only, bit 1
+ * key-value) and every size class, builds a batch of segments of the class's
+ * size (delta identifier, about keys_per_trial keys in all), times each valid
+ * variant as a graph replay on `stream` (best of `reps`) and stores the fastest
+ * in the table.  It allocates its own device buffers (about 16 bytes per
+ * trial key) and frees them before returning; it synchronises `stream`.
+ * h_ms_out (optional) receives the best time per entry, indexed
+ * [(k-1) * 2 + key_value] * GMS_NUM_SIZE_CLASSES + size_class (16 * 8 floats). */
+gms_status gms_autotune(uint32_t bucket_mask, uint32_t key_value_mask, uint32_t keys_per_trial, int reps,
+                        float* h_ms_out, gms_stream_t stream);
 
 /* -------------------------------------------------------------- serving */
 /* A request loop with continuous batching.  No reference counterpart.  A

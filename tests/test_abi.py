@@ -108,6 +108,87 @@ def test_sort_scratch_covers_both_digit_widths(gms_lib):
             assert sb.value >= max(m16, m128) + 4 * n * (1 + kv)
 
 
+def test_sort_scratch_all_digit_widths(gms_lib):
+    """The sort scratch holds the widest pass's count matrix plus the ping-pong buffers."""
+    widths = {4: (16,), 5: (32, 4), 6: (16, 64), 7: (16, 128), 8: (256,)}
+    for bits, bs in widths.items():
+        for n in (1, 4097, 1 << 20):
+            for kv in (0, 1):
+                sb = ctypes.c_size_t()
+                assert gms_lib.gms_sort_scratch_bytes(n, bits, kv, ctypes.byref(sb)) == 0
+                need = max(scratch_bytes(n, b, kv)[1] for b in bs) + 4 * n * (1 + kv)
+                assert sb.value >= need, (bits, n, kv)
+    sb = ctypes.c_size_t()
+    for bad in (3, 9, 0):
+        assert gms_lib.gms_sort_scratch_bytes(100, bad, 0, ctypes.byref(sb)) == _lib.GMS_ERROR_INVALID_VALUE
+
+
+def test_tuning_table_host_logic(gms_lib):
+    """Tile variants, the built-in table, set/get/reset and their checks (host only)."""
+    from gpumultisplit_gb300 import batched
+
+    shapes = [gms.tile_variant_shape(v) for v in range(batched.NUM_TILE_VARIANTS)]
+    assert shapes[0] == (8, 16, 4096)
+    assert all(t == w * 32 * i for w, i, t in shapes)
+    gms.reset_tuning()
+    base = gms.tuning_table()
+    # built-in: the tile that holds the segment up to 2048 keys, the 4096-key tile above
+    for (b, kv, c), v in base.items():
+        assert gms.tile_variant_shape(v)[2] == {0: 1024, 1: 2048}.get(c, 4096)
+    assert [batched.size_class(n) for n in (0, 1, 1024, 1025, 2048, 2049, 65536, 65537, 1 << 30)] == \
+        [0, 0, 0, 1, 1, 2, 6, 7, 7]
+    gms.set_tuning({(128, True, 3): 3})
+    assert gms.tuning_table()[(128, True, 3)] == 3
+    v = ctypes.c_int()
+    assert gms_lib.gms_tuning_set(256, 1, 3, 3) == _lib.GMS_ERROR_INVALID_VALUE  # 128 threads < 256 buckets
+    assert gms_lib.gms_tuning_set(256, 1, 8, 0) == _lib.GMS_ERROR_INVALID_VALUE  # no size class 8
+    assert gms_lib.gms_tuning_set(3, 1, 0, 0) == _lib.GMS_ERROR_UNSUPPORTED_BUCKETS
+    assert gms_lib.gms_tuning_get(512, 0, 0, ctypes.byref(v)) == _lib.GMS_ERROR_UNSUPPORTED_BUCKETS
+    assert gms_lib.gms_tile_variant_shape(4, None, None, None) == _lib.GMS_ERROR_INVALID_VALUE
+    gms.reset_tuning()
+    assert gms.tuning_table() == base
+    # autotune argument checks fail before any CUDA call
+    assert gms_lib.gms_autotune(1, 1, 1 << 20, 1, None, None) == _lib.GMS_ERROR_INVALID_VALUE    # bit 0 = 1 bucket
+    assert gms_lib.gms_autotune(4, 0, 1 << 20, 1, None, None) == _lib.GMS_ERROR_INVALID_VALUE    # no shape
+    assert gms_lib.gms_autotune(4, 1, 1000, 1, None, None) == _lib.GMS_ERROR_INVALID_VALUE       # too few keys
+    assert gms_lib.gms_autotune(4, 1, 1 << 20, 0, None, None) == _lib.GMS_ERROR_INVALID_VALUE    # no repetitions
+
+
+def test_batch_plan_classes_follow_the_table(gms_lib):
+    """Plans are host-only: launches = 2 per (kind, B, key/value, variant) class + 1 scan."""
+    from gpumultisplit_gb300 import batched
+
+    gms.reset_tuning()
+    fake = 1 << 32  # never dereferenced: plan creation does no device work
+
+    def plan(sizes, B=256, variant=None):
+        arr = (batched.GmsSegment * len(sizes))()
+        for i, n in enumerate(sizes):
+            arr[i] = batched.GmsSegment(fake, fake, fake, fake, n, gms.delta_bucket().desc(B))
+        h = ctypes.c_void_p()
+        if variant is None:
+            st = gms_lib.gms_batch_create(arr, len(sizes), ctypes.byref(h))
+        else:
+            st = gms_lib.gms_batch_create_with_variant(arr, len(sizes), variant, ctypes.byref(h))
+        assert st == 0
+        n = ctypes.c_uint32()
+        assert gms_lib.gms_batch_launch_count(h, ctypes.byref(n)) == 0
+        gms_lib.gms_batch_destroy(h)
+        return n.value
+
+    assert plan([1000, 1000, 5000]) == 2 * 2 + 1        # 1024-key tiles and 4096-key tiles
+    assert plan([1000, 1500, 5000]) == 2 * 3 + 1
+    assert plan([1000, 1500, 5000], variant=0) == 2 + 1
+    gms.set_tuning({(256, True, c): 0 for c in range(8)})
+    assert plan([1000, 1500, 5000]) == 2 + 1
+    gms.reset_tuning()
+    arr = (batched.GmsSegment * 1)()
+    arr[0] = batched.GmsSegment(fake, fake, fake, fake, 10, gms.delta_bucket().desc(256))
+    h = ctypes.c_void_p()
+    assert gms_lib.gms_batch_create_with_variant(arr, 1, 3, ctypes.byref(h)) == _lib.GMS_ERROR_INVALID_VALUE
+    assert gms_lib.gms_batch_create_with_variant(arr, 1, -1, ctypes.byref(h)) == _lib.GMS_ERROR_INVALID_VALUE
+
+
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(ImportError):
         _lib.load(tmp_path / "libgpumultisplit.so")

@@ -58,7 +58,11 @@ def test_batched_equals_plain_path_and_replays(gms_lib, oracle_mod):
     sizes = np.exp(rng.uniform(np.log(1024), np.log(1 << 18), 200)).astype(np.int64)
     segs, refs = make_segments(oracle_mod, sizes, 7)
     plan = gms.BatchedMultisplit(segs)
-    assert plan.launches <= 2 * 8 + 2
+    # one prescan and one postscan per (kind, B, key/value, tile variant) class, one scan
+    table = gms.tuning_table()
+    classes = {(s.identifier.desc(s.num_buckets).kind, s.num_buckets,
+                table[(s.num_buckets, True, gms.batched.size_class(s.n))]) for s in segs}
+    assert plan.launches == 2 * len(classes) + 1
     for _ in range(3):
         for s in segs:
             s.keys_out.zero_()
@@ -88,3 +92,49 @@ def test_batched_empty_plan(gms_lib):
     plan = gms.BatchedMultisplit([])
     plan.run()
     plan.close()
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_batched_each_tile_variant_matches_oracle(gms_lib, oracle_mod, variant):
+    """Every tile shape the tuning table can pick gives the oracle's output."""
+    warps, ipt, tile = gms.tile_variant_shape(variant)
+    assert tile == warps * 32 * ipt
+    buckets = tuple(b for b in (2, 8, 32, 128, 256) if b <= warps * 32)
+    sizes = [1, 700, 1024, 1025, 2048, 2049, 4097, 30000, 70001, 0, 5]
+    segs, refs = make_segments(oracle_mod, sizes, 11 + variant, kinds=(0, 2, 3, 5), buckets=buckets,
+                               kv_pattern=(1, 0))
+    plan = gms.BatchedMultisplit(segs, variant=variant)
+    plan.run(use_graph=True)
+    torch.cuda.synchronize()
+    assert plan.device_error() == 0
+    check_against_oracle(oracle_mod, segs, refs)
+    plan.close()
+
+
+def test_batched_variant_needs_a_thread_per_bucket(gms_lib):
+    k = torch.zeros(10, dtype=torch.int32, device="cuda")
+    with pytest.raises(gms.GmsError):
+        gms.BatchedMultisplit([gms.Segment(k, k.clone(), 10, 256, gms.delta_bucket())], variant=3)
+
+
+def test_autotune_fills_table_and_keeps_outputs(gms_lib, oracle_mod):
+    """The autotuner times every class, stores valid variants, and a plan built
+    from the tuned table still gives the oracle's output."""
+    gms.reset_tuning()
+    try:
+        ms = gms.autotune(buckets=(2, 256), key_value=(False, True), keys_per_trial=1 << 20, reps=1)
+        assert len(ms) == 2 * 2 * gms.batched.NUM_SIZE_CLASSES
+        assert all(t > 0 for t in ms.values())
+        table = gms.tuning_table()
+        for (b, kv, c), v in table.items():
+            assert gms.tile_variant_shape(v)[0] * 32 >= b
+        sizes = [1, 900, 1500, 3000, 9000, 40000, 200000]
+        segs, refs = make_segments(oracle_mod, sizes, 17, kinds=(0, 3), buckets=(2, 256), kv_pattern=(1, 0, 1))
+        plan = gms.BatchedMultisplit(segs)
+        plan.run(use_graph=True)
+        torch.cuda.synchronize()
+        assert plan.device_error() == 0
+        check_against_oracle(oracle_mod, segs, refs)
+        plan.close()
+    finally:
+        gms.reset_tuning()
