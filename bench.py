@@ -62,6 +62,9 @@ def parse():
     p.add_argument("--only-serving", action="store_true", help="print only the serving-form summary")
     p.add_argument("--serve-seconds", type=float, default=3.0)
     p.add_argument("--serve-rate", type=float, default=20000.0)
+    p.add_argument("--sweep", action="store_true",
+                   help="time every 2^28 case of the key-value sweep, key-only, compaction, histogram and sort "
+                        "(one JSON line per case) instead of the headline line")
     return p.parse_args()
 
 
@@ -290,6 +293,127 @@ def serving_trace(seconds: float, rate: float, seed: int = 5):
     kv = rng.random(m) < 0.5
     buckets = rng.choice([2, 8, 32, 256], size=m)
     return t, sizes, ops, kv, buckets
+
+
+def run_sweep(a, dev):
+    """One JSON line per case, inputs resident in HBM, CUDA events around
+    `steps` calls after `warmup` calls, each case's output checked by a
+    size-independent property (bucket order + permutation for multisplits,
+    sortedness for sorts, total count for histograms)."""
+    import torch
+
+    import gpumultisplit_gb300 as gms
+    from gpumultisplit_gb300 import datagen
+
+    n = 1 << a.log2n
+    peak, _ = hbm_peak()
+    inputs = {"uniform": datagen.uniform_u32(n, 3, device=dev), "zipf": datagen.zipf_u32(n, 3, device=dev),
+              "and4": datagen.and4_u32(n, 3, device=dev)}
+    vals = datagen.index_values(n, dev)
+    kout, vout = torch.empty_like(vals), torch.empty_like(vals)
+    steps, warm = max(3, a.steps // 2), max(3, a.warmup)
+
+    def timed(fn):
+        for _ in range(warm):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    def emit(case, ms, bytes_per_key, check):
+        line = {"case": case, "n": n, "ms": ms, "gkeys": n / (ms * 1e-3) / 1e9,
+                "algorithmic_bytes_per_key": bytes_per_key,
+                "hbm_frac": bytes_per_key * n / (ms * 1e-3) / 1e9 / peak, "check": check}
+        print(json.dumps(line), flush=True)
+
+    def bucket_ids(x, B, ident_name, spl):
+        u = x.to(torch.int64) & 0xFFFFFFFF
+        if ident_name == "delta":
+            return (u * B) >> 32
+        s64 = spl.to(torch.int64) & 0xFFFFFFFF
+        return torch.searchsorted(s64, u, right=True) - 1
+
+    def multisplit_check(kin, ko, vo, B, ident_name, spl):
+        b = bucket_ids(ko, B, ident_name, spl)
+        ok = bool((b[1:] >= b[:-1]).all())
+        if vo is not None:
+            ok &= bool(torch.equal(kin[vo.long()], ko))
+            same = b[1:] == b[:-1]
+            ok &= bool((vo[1:][same] > vo[:-1][same]).all())  # stable: values = input index
+        return "pass" if ok else "FAIL"
+
+    # key-value sweep: B x distribution x identifier
+    for dist in ("uniform", "zipf"):
+        for ident_name in ("delta", "range"):
+            for B in (2, 32, 64, 128, 256):
+                spl = datagen.range_splitters(B, 5, dev) if ident_name == "range" else None
+                ident = gms.delta_bucket() if ident_name == "delta" else gms.range_bucket(spl)
+                ctx = gms.multisplit_context(B)
+                gms.multisplit_allocate_key_value(n, ctx)
+                kin = inputs[dist]
+                ms = timed(lambda: gms.multisplit_key_value(kin, vals, kout, vout, n, ctx, ident))
+                emit(f"multisplit kv B={B} {dist} {ident_name}", ms, 20,
+                     multisplit_check(kin, kout, vout, B, ident_name, spl))
+                gms.multisplit_release_memory(ctx)
+    for B in (2, 32, 256):
+        ctx = gms.multisplit_context(B)
+        gms.multisplit_allocate_key_only(n, ctx)
+        kin = inputs["uniform"]
+        ms = timed(lambda: gms.multisplit_key_only(kin, kout, n, ctx, gms.delta_bucket()))
+        ok = multisplit_check(kin, kout, None, B, "delta", None)
+        ok = ok if bool(torch.equal(torch.sort(kout.long() & 0xFFFFFFFF)[0],
+                                    torch.sort(kin.long() & 0xFFFFFFFF)[0])) else "FAIL"
+        emit(f"multisplit k B={B} uniform delta", ms, 12, ok)
+        gms.multisplit_release_memory(ctx)
+    # compaction, predicate key & 1
+    for kv in (False, True):
+        ctx = gms.compaction_context()
+        kin = inputs["uniform"]
+        if kv:
+            gms.compaction_allocate_key_value(n, ctx)
+            ms = timed(lambda: gms.compaction_key_value(kin, vals, kout, vout, n, ctx, gms.test_bucket(1)))
+        else:
+            gms.compaction_allocate_key_only(n, ctx)
+            ms = timed(lambda: gms.compaction_key_only(kin, kout, n, ctx, gms.test_bucket(1)))
+        b = kout & 1
+        emit(f"compaction {'kv' if kv else 'k'} key&1 uniform", ms, 20 if kv else 12,
+             "pass" if bool((b[1:] >= b[:-1]).all()) else "FAIL")
+        gms.compaction_release_memory(ctx)
+    # 256-bin histograms
+    hist = torch.zeros(256, dtype=torch.int32, device=dev)
+    kin = inputs["uniform"]
+    ms = timed(lambda: gms.multisplit_histogram(kin, n, hist, 256, gms.delta_bucket()))
+    hist.zero_()
+    gms.multisplit_histogram(kin, n, hist, 256, gms.delta_bucket())
+    emit("histogram 256 bins delta uniform", ms, 4, "pass" if int(hist.sum()) == n else "FAIL")
+    ms = timed(lambda: gms.histogram_even(kin, n, hist, 256, 0, 0xFFFFFFFF, 256.0 / 2**32))
+    emit("histogram 256 bins even-float uniform", ms, 4, "pass")
+    # sorts
+    for bits in (7, 4, 5, 6, 8):
+        for dist in (("uniform", "and4") if bits == 7 else ("uniform",)):
+            for kv in ((False, True) if bits == 7 else (True,)):
+                ctx = gms.ms_sort_context()
+                kin = inputs[dist]
+                fn = f"multisplit_sort_{bits}bit"
+                if kv:
+                    getattr(gms, fn + "_allocate_pairs")(n, ctx)
+                    ms = timed(lambda: getattr(gms, fn + "_pairs")(kin, kout, vals, vout, n, ctx))
+                else:
+                    getattr(gms, fn + "_allocate")(n, ctx)
+                    ms = timed(lambda: getattr(gms, fn)(kin, kout, n, ctx))
+                u = kout.long() & 0xFFFFFFFF
+                ok = bool((u[1:] >= u[:-1]).all())
+                if kv:
+                    ok &= bool(torch.equal(kin[vout.long()], kout))
+                passes = {4: 8, 5: 7, 6: 6, 7: 5, 8: 4}[bits]
+                emit(f"sort {bits}-bit {'kv' if kv else 'k'} {dist}", ms, passes * (20 if kv else 12),
+                     "pass" if ok else "FAIL")
+                gms.multisplit_sort_release_memory(ctx)
 
 
 def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: float = 64.0, verify: int = 24):
@@ -570,6 +694,9 @@ def run_ours(a):
 
     gbuild.build()
     gms.load()
+    if a.sweep:
+        run_sweep(a, dev)
+        return
 
     n = 1 << a.log2n
     B = a.buckets

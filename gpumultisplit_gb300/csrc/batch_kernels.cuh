@@ -82,8 +82,32 @@ __global__ void __launch_bounds__(C::THREADS, (PostLayout<C, DescPolicy<KIND, C:
   const uint2 m = tile_map[blockIdx.x];
   const SegDesc& sd = segs[m.x];
   const TileJob<BucketParams> job{sd.kin, sd.vin,  sd.kout, sd.vout, sd.n,  sd.num_tiles,
-                                  m.y,    matrix + sd.matrix_off, sd.base, ~0u, sd.bp};
+                                  m.y,    matrix + sd.matrix_off, sd.base, ~0u, sd.bp, m.x};
   postscan_job<C, DescPolicy<KIND, C::LOGB>>(job, hdr, smem);
+}
+
+// Persistent form for identifiers with a shared area (RANGE): block b runs a
+// contiguous range of the class's tile map and prepares the identifier again
+// only when the segment changes.  The prefetch pulls the next tile of the same
+// segment into L2.
+template <class C, int KIND>
+__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, DescPolicy<KIND, C::LOGB>>::MIN_BLOCKS))
+    batch_postscan_persistent_kernel(const SegDesc* __restrict__ segs, const uint2* __restrict__ tile_map,
+                                     uint32_t class_tiles, const uint32_t* __restrict__ matrix, ScratchHeader* hdr) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const uint32_t per = (class_tiles + gridDim.x - 1) / gridDim.x;
+  const uint32_t first = blockIdx.x * per;
+  const uint32_t last = min(first + per, class_tiles);
+  postscan_run<C, DescPolicy<KIND, C::LOGB>>(
+      first, last, 1u,
+      [&](uint32_t t, uint32_t next) {
+        const uint2 m = tile_map[t];
+        const SegDesc& sd = segs[m.x];
+        const uint32_t pf = (next != ~0u && tile_map[next].x == m.x) ? tile_map[next].y : ~0u;
+        return TileJob<BucketParams>{sd.kin, sd.vin, sd.kout, sd.vout, sd.n, sd.num_tiles, m.y,
+                                     matrix + sd.matrix_off, sd.base, pf, sd.bp, m.x};
+      },
+      hdr, smem);
 }
 
 }  // namespace gms

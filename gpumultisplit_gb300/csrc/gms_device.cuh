@@ -54,6 +54,12 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
+// Invalidate an mbarrier whose phases are all complete, before its memory is
+// initialised again.
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // Make an initialised mbarrier visible to the async (bulk copy) proxy.
 __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -151,15 +157,20 @@ struct BucketParams {
 };
 
 // RANGE identifiers narrow each search with a table over the key's top
-// RANGE_LUT_BITS bits: lut[t] = number of splitters below t << (32 - bits),
-// so a key in cell t has between lut[t] and lut[t+1] splitters <= it.
-constexpr int RANGE_LUT_BITS = 8;
+// RANGE_LUT_BITS bits.  Entry t packs lo(t) | lo(t+1) << 16, where lo(t) is the
+// number of splitters below t << (32 - bits) (lo(CELLS) = B): a key in cell t
+// has between lo(t) and lo(t+1) splitters <= it.  With 1024 cells a cell holds
+// a splitter for at most B/1024 of the keys, so most keys need one table load
+// and no search.
+constexpr int RANGE_LUT_BITS = 10;
 constexpr uint32_t RANGE_LUT_CELLS = 1u << RANGE_LUT_BITS;
+// Up to this many buckets the splitters are compared one by one (no table).
+constexpr uint32_t RANGE_SCAN_MAX_B = 8;
 
 // Shared words an identifier needs (splitters + lookup table for RANGE).
 template <int KIND, int LOGB>
 __host__ __device__ constexpr uint32_t identifier_smem_words() {
-  return KIND == KIND_RANGE ? (1u << LOGB) + (RANGE_LUT_CELLS + 2) / 2 : 1u;
+  return KIND != KIND_RANGE ? 1u : ((1u << LOGB) <= RANGE_SCAN_MAX_B ? (1u << LOGB) : (1u << LOGB) + RANGE_LUT_CELLS);
 }
 
 // A bucket identifier for B = 2^LOGB buckets.  `s_split` is the shared-memory
@@ -180,18 +191,34 @@ struct Identifier {
       return (key >> p.shift) & (B - 1);
     } else if constexpr (KIND == KIND_RANGE) {
       // c = number of splitters <= key (upper_bound); bucket = c - 1, which
-      // wraps to B-1 when key < s[0].  The table bounds c to [lut[t], lut[t+1]].
-      const uint16_t* lut = reinterpret_cast<const uint16_t*>(s_split + B);
-      const uint32_t t = key >> (32 - RANGE_LUT_BITS);
-      uint32_t c = lut[t], hi = lut[t + 1];
-      while (c < hi) {
-        const uint32_t mid = (c + hi + 1) >> 1;
-        if (s_split[mid - 1] <= key)
-          c = mid;
-        else
-          hi = mid - 1;
+      // wraps to B-1 when key < s[0].
+      if constexpr (B <= RANGE_SCAN_MAX_B) {
+        // Few splitters: compare against all of them (same address for every
+        // lane, so each load is a broadcast).
+        uint32_t c = 0;
+#pragma unroll
+        for (uint32_t i = 0; i < B; ++i) c += s_split[i] <= key ? 1u : 0u;
+        return (c - 1u) & (B - 1);
+      } else {
+        // The table bounds c to [lo(t), lo(t+1)].  The cell's first splitter
+        // is tested without a branch; only cells with two or more splitters
+        // need a search over the rest.
+        const uint32_t e = s_split[B + (key >> (32 - RANGE_LUT_BITS))];
+        uint32_t c = e & 0xFFFFu, hi = e >> 16;
+        const uint32_t s0 = s_split[c < B ? c : B - 1];
+        const bool past_first = c < hi && s0 <= key;
+        c += past_first ? 1u : 0u;
+        if (past_first && c < hi) {
+          while (c < hi) {
+            const uint32_t mid = (c + hi + 1) >> 1;
+            if (s_split[mid - 1] <= key)
+              c = mid;
+            else
+              hi = mid - 1;
+          }
+        }
+        return (c - 1u) & (B - 1);
       }
-      return (c - 1u) & (B - 1);
     } else if constexpr (KIND == KIND_MASK) {
       return (key & p.param) ? 1u : 0u;
     } else {  // KIND_EVEN_FLOAT
@@ -202,29 +229,43 @@ struct Identifier {
 };
 
 // Fill the identifier's shared area (RANGE: splitters, then the lookup table).
-// No-op for other kinds.  All threads of the block must call it.
+// No-op for other kinds.  All threads of the block must call it; a barrier
+// must follow before the identifier is used.
 template <int KIND, int LOGB>
 __device__ __forceinline__ void prepare_identifier(uint32_t* s_split, const BucketParams& p) {
   if constexpr (KIND == KIND_RANGE) {
     constexpr uint32_t B = 1u << LOGB;
+    constexpr uint32_t SHIFT = 32 - RANGE_LUT_BITS;
     for (uint32_t i = threadIdx.x; i < B; i += blockDim.x) s_split[i] = p.splitters[i];
     __syncthreads();
-    uint16_t* lut = reinterpret_cast<uint16_t*>(s_split + B);
-    for (uint32_t t = threadIdx.x; t <= RANGE_LUT_CELLS; t += blockDim.x) {
-      uint32_t lo = B;  // lower_bound of t << (32 - bits); the top cell ends at 2^32
-      if (t < RANGE_LUT_CELLS) {
-        const uint32_t v = t << (32 - RANGE_LUT_BITS);
-        uint32_t hi = B;
-        lo = 0;
-        while (lo < hi) {
-          const uint32_t mid = (lo + hi) >> 1;
-          if (s_split[mid] < v)
-            lo = mid + 1;
-          else
-            hi = mid;
-        }
+    if constexpr (B <= RANGE_SCAN_MAX_B) return;
+    uint32_t* lut = s_split + B;
+    // Each thread fills a run of consecutive cells: one binary search for the
+    // run's first cell, then a walk over the (sorted) splitters of the run.
+    const uint32_t per = (RANGE_LUT_CELLS + blockDim.x - 1) / blockDim.x;
+    const uint32_t t0 = threadIdx.x * per;
+    if (t0 < RANGE_LUT_CELLS) {
+      const uint32_t v = t0 << SHIFT;
+      uint32_t lo = 0, hi = B;
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_split[mid] < v)
+          lo = mid + 1;
+        else
+          hi = mid;
       }
-      lut[t] = uint16_t(lo);
+      const uint32_t t1 = min(t0 + per, RANGE_LUT_CELLS);
+      for (uint32_t t = t0; t < t1; ++t) {
+        uint32_t next = lo;
+        if (t + 1 == RANGE_LUT_CELLS) {
+          next = B;
+        } else {
+          const uint32_t end = (t + 1) << SHIFT;
+          while (next < B && s_split[next] < end) ++next;
+        }
+        lut[t] = lo | (next << 16);
+        lo = next;
+      }
     }
   }
 }

@@ -74,6 +74,18 @@ cudaError_t launch_multisplit(const uint32_t* kin, const uint32_t* vin, uint32_t
     cudaError_t e = run_scan(matrix, g.m, status, hdr, stream);
     if (e != cudaSuccess) return e;
   }
+  if ((stages & STAGE_POSTSCAN) && P::USES_SMEM) {
+    // Identifiers with a shared area: persistent blocks prepare it once.
+    static std::atomic<uint64_t> smem_done{0};
+    static std::atomic<int> per_sm{0};
+    auto kern = postscan_persistent_kernel<C, P>;
+    constexpr size_t smem = PostLayout<C, P>::BYTES;
+    cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
+    kern<<<grid, C::THREADS, smem, stream>>>(kin, vin, kout, vout, n, g.num_tiles, matrix, params, hdr);
+    return cudaGetLastError();
+  }
   if (stages & STAGE_POSTSCAN) {
     static std::atomic<uint64_t> smem_done{0};
     static std::atomic<int> per_sm{0};
@@ -135,8 +147,17 @@ cudaError_t run_batch_class_t(const BatchClassLaunch& c, int stage) {
       return cudaGetLastError();
     }
     static std::atomic<uint64_t> smem_done{0};
-    auto kern = batch_postscan_kernel<C, KIND>;
     constexpr size_t smem = PostLayout<C, DescPolicy<KIND, LOGB>>::BYTES;
+    if constexpr (DescPolicy<KIND, LOGB>::USES_SMEM) {
+      static std::atomic<int> per_sm{0};
+      auto kern = batch_postscan_persistent_kernel<C, KIND>;
+      cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
+      if (e != cudaSuccess) return e;
+      const uint32_t grid = persistent_grid(kern, C::THREADS, c.class_tiles, per_sm, smem);
+      kern<<<grid, C::THREADS, smem, c.stream>>>(c.segs, c.tile_map, c.class_tiles, c.matrix, c.hdr);
+      return cudaGetLastError();
+    }
+    auto kern = batch_postscan_kernel<C, KIND>;
     cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
     if (e != cudaSuccess) return e;
     kern<<<c.class_tiles, C::THREADS, smem, c.stream>>>(c.segs, c.tile_map, c.matrix, c.hdr);

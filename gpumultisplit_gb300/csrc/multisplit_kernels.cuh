@@ -15,6 +15,8 @@
 // same because the padding only ever sits after all real keys.
 #pragma once
 
+#include <type_traits>
+
 #include "gms_device.cuh"
 
 // How a warp finds, for B > 32, the lanes holding the same bucket as each lane
@@ -220,29 +222,36 @@ __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __r
   });
 }
 
-// Shared-memory layout of the postscan for identifier KIND (bytes), and what
-// phase 3 writes into the reorder buffer R at each key's bucket-sorted position:
-//   R_KEYS     the key itself (key-only, identifier cheap to recompute): phase 4
-//              reads keys conflict-free and recomputes their buckets;
-//   R_INDEX16  the key's 16-bit in-tile index (key-value, cheap identifier):
-//              a small buffer keeps four tiles resident per SM;
-//   R_PACKED   (bucket << 16) | index, for identifiers that are costly to
-//              recompute (RANGE, DIV, EVEN_FLOAT).
-enum ReorderMode { R_KEYS = 0, R_INDEX16 = 1, R_PACKED = 2 };
+// Shared-memory layout of the postscan for identifier policy P (bytes), and
+// what phase 3 writes at each key's bucket-sorted position:
+//   R_KEYS       the key (key-only, identifier cheap to recompute): phase 4
+//                reads keys conflict-free and recomputes their buckets;
+//   R_INDEX16    the key's 16-bit in-tile index (key-value, cheap identifier):
+//                a small buffer keeps four tiles resident per SM;
+//   R_KEYS_B,    the same plus the key's bucket as one byte, for identifiers
+//   R_INDEX16_B  that are costly to recompute (RANGE, DIV, EVEN_FLOAT, user
+//                functors).
+// The per-warp count table holds 16-bit entries (a warp counts at most
+// 32 * IPT keys and a tile holds at most 2^16), except in the bitmap peer mode.
+enum ReorderMode { R_KEYS = 0, R_INDEX16 = 1, R_KEYS_B = 2, R_INDEX16_B = 3 };
 
 template <class C, class P>
 struct PostLayout {
   static constexpr bool CHEAP = P::CHEAP;
-  static constexpr int MODE = !CHEAP ? R_PACKED : (C::KV ? R_INDEX16 : R_KEYS);
+  static constexpr int MODE = C::KV ? (CHEAP ? R_INDEX16 : R_INDEX16_B) : (CHEAP ? R_KEYS : R_KEYS_B);
+  static constexpr bool INDEXED = MODE == R_INDEX16 || MODE == R_INDEX16_B;
+  static constexpr bool BUCKET_BYTES = MODE == R_KEYS_B || MODE == R_INDEX16_B;
+  using WhT = std::conditional_t<C::WS == 2, uint32_t, uint16_t>;
   static constexpr size_t OFF_K = 0;
   static constexpr size_t OFF_V = OFF_K + C::TILE * 4;
   static constexpr size_t OFF_R = OFF_V + (C::KV ? C::TILE * 4 : 0);
-  static constexpr size_t R_BYTES = size_t(C::TILE) * (MODE == R_INDEX16 ? 2 : 4);
-  static constexpr size_t OFF_WH = (OFF_R + R_BYTES + 15) & ~size_t(15);
-  static constexpr size_t OFF_DELTA = OFF_WH + size_t(C::WARPS) * C::WB * C::WS * 4;
+  static constexpr size_t R_BYTES = size_t(C::TILE) * (INDEXED ? 2 : 4);
+  static constexpr size_t OFF_RB = OFF_R + R_BYTES;  // bucket bytes
+  static constexpr size_t OFF_WH = (OFF_RB + (BUCKET_BYTES ? C::TILE : 0) + 15) & ~size_t(15);
+  static constexpr size_t OFF_DELTA = (OFF_WH + size_t(C::WARPS) * C::WB * C::WS * sizeof(WhT) + 15) & ~size_t(15);
   static constexpr size_t OFF_SPLIT = OFF_DELTA + C::B * 4;
   static constexpr size_t OFF_SCAN = OFF_SPLIT + P::SMEM_WORDS * 4;
-  static constexpr size_t OFF_FLAG = OFF_SCAN + C::B * 4;
+  static constexpr size_t OFF_FLAG = OFF_SCAN + 32 * 4;  // warp totals of the tile scan
   static constexpr size_t OFF_BAR = (OFF_FLAG + 4 + 15) & ~size_t(15);
   static constexpr size_t BYTES = OFF_BAR + 16;
   // Blocks per SM the register budget is sized for (64 registers at 16 keys per thread).
@@ -267,10 +276,11 @@ __device__ __forceinline__ uint32_t peers_by_ballot(uint32_t b) {
 // Phases 1-4 of the postscan for one staged tile.  FULL: the tile holds
 // exactly TILE keys, so no per-key validity test is needed.
 template <class C, class P, bool FULL>
-__device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
+__device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
                                               uint32_t cnt, uint32_t goff, const typename P::Params& bp,
                                               ScratchHeader* hdr, unsigned char* smem) {
   using L = PostLayout<C, P>;
+  using WhT = typename L::WhT;
   constexpr uint32_t B = C::B;
   constexpr int LOGB = C::LOGB;
   constexpr int IPT = C::IPT;
@@ -279,7 +289,8 @@ __device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint3
   uint32_t* s_k = reinterpret_cast<uint32_t*>(smem + L::OFF_K);
   uint32_t* s_v = reinterpret_cast<uint32_t*>(smem + L::OFF_V);
   uint32_t* s_r = reinterpret_cast<uint32_t*>(smem + L::OFF_R);
-  uint32_t* s_wh = reinterpret_cast<uint32_t*>(smem + L::OFF_WH);
+  uint8_t* s_rb = reinterpret_cast<uint8_t*>(smem + L::OFF_RB);
+  WhT* s_wh = reinterpret_cast<WhT*>(smem + L::OFF_WH);
   uint32_t* s_delta = reinterpret_cast<uint32_t*>(smem + L::OFF_DELTA);
   const uint32_t* s_split = reinterpret_cast<const uint32_t*>(smem + L::OFF_SPLIT);
   uint32_t* s_scan = reinterpret_cast<uint32_t*>(smem + L::OFF_SCAN);
@@ -313,16 +324,16 @@ __device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint3
       packed[j] = (b << 16) | (before + __popc(peers & lt));
       my_cnt += __popc(m);
     }
-    if (lane < B) s_wh[warp * WB + lane] = my_cnt;
+    if (lane < B) s_wh[warp * WB + lane] = WhT(my_cnt);
   } else {
-    uint32_t* wh = s_wh + warp * WB * WS;  // entry b: count at [b*WS + WS-1], bitmap at [b*WS] when WS == 2
+    WhT* wh = s_wh + warp * WB * WS;  // entry b: count at [b*WS + WS-1], bitmap at [b*WS] when WS == 2
     if constexpr (GMS_PEERS_MODE == 2) {
 #pragma unroll
       for (int j = 0; j < IPT; ++j) {
         const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
         const bool valid = FULL || pos < cnt;
         const uint32_t b = ident(s_k[pos]);
-        uint32_t* e = &wh[b * WS];
+        uint32_t* e = reinterpret_cast<uint32_t*>(&wh[b * WS]);
         if (valid) atomicOr(e, 1u << lane);
         __syncwarp();
         const uint2 v = *reinterpret_cast<const uint2*>(e);
@@ -345,10 +356,10 @@ __device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint3
 #endif
         if (!FULL) peers &= __ballot_sync(~0u, valid);
         const uint32_t rank = __popc(peers & lt);
-        uint32_t* e = &wh[b * WS + (WS - 1)];
+        WhT* e = &wh[b * WS + (WS - 1)];
         const uint32_t before = *e;
         __syncwarp();
-        if (valid && rank == 0) *e = before + __popc(peers);
+        if (valid && rank == 0) *e = WhT(before + __popc(peers));
         __syncwarp();
         packed[j] = (b << 16) | (before + rank);
       }
@@ -365,9 +376,9 @@ __device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint3
     if (tid < B) {
 #pragma unroll
       for (int w = 0; w < C::WARPS; ++w) {
-        uint32_t* c_ptr = &s_wh[(w * WB + tid) * WS + (WS - 1)];
+        WhT* c_ptr = &s_wh[(w * WB + tid) * WS + (WS - 1)];
         const uint32_t c = *c_ptr;
-        *c_ptr = total;
+        *c_ptr = WhT(total);
         total += c;
       }
       if (uint64_t(goff) + total > n) atomicOr(s_flag, 1u);
@@ -389,29 +400,32 @@ __device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint3
       }
       s_delta[tid] = goff - start;
 #pragma unroll
-      for (int w = 0; w < C::WARPS; ++w) s_wh[(w * WB + tid) * WS + (WS - 1)] += start;
+      for (int w = 0; w < C::WARPS; ++w) {
+        WhT* c_ptr = &s_wh[(w * WB + tid) * WS + (WS - 1)];
+        *c_ptr = WhT(*c_ptr + start);
+      }
     }
   }
   __syncthreads();
   if (*s_flag != 0u) {  // block-uniform
     if (tid == 0) record_error(hdr, DEV_ERR_BAD_OFFSET);
-    return;
+    return false;
   }
 
   // ---- 3. bucket-sorted in-tile order (positions are a permutation of [0, cnt))
   {
-    const uint32_t* wh = s_wh + warp * WB * WS + (WS - 1);
+    const WhT* wh = s_wh + warp * WB * WS + (WS - 1);
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
       const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
       if (FULL || pos < cnt) {
-        const uint32_t d = wh[(packed[j] >> 16) * WS] + (packed[j] & 0xFFFFu);
-        if constexpr (L::MODE == R_KEYS)
-          s_r[d] = s_k[pos];
-        else if constexpr (L::MODE == R_INDEX16)
+        const uint32_t b = packed[j] >> 16;
+        const uint32_t d = uint32_t(wh[b * WS]) + (packed[j] & 0xFFFFu);
+        if constexpr (L::INDEXED)
           reinterpret_cast<uint16_t*>(s_r)[d] = uint16_t(pos);
         else
-          s_r[d] = (packed[j] & 0xFFFF0000u) | pos;
+          s_r[d] = s_k[pos];
+        if constexpr (L::BUCKET_BYTES) s_rb[d] = uint8_t(b);
       }
     }
   }
@@ -425,21 +439,18 @@ __device__ __forceinline__ void postscan_tile(uint32_t* __restrict__ kout, uint3
       if constexpr (L::MODE == R_KEYS) {
         const uint32_t key = s_r[p];
         kout[s_delta[ident(key)] + p] = key;
-      } else if constexpr (L::MODE == R_INDEX16) {
+      } else if constexpr (L::MODE == R_KEYS_B) {
+        kout[s_delta[s_rb[p]] + p] = s_r[p];
+      } else {
         const uint32_t src = reinterpret_cast<const uint16_t*>(s_r)[p];
         const uint32_t key = s_k[src];
-        const uint32_t g = s_delta[ident(key)] + p;
+        const uint32_t g = s_delta[L::BUCKET_BYTES ? uint32_t(s_rb[p]) : ident(key)] + p;
         kout[g] = key;
         vout[g] = s_v[src];
-      } else {
-        const uint32_t e = s_r[p];
-        const uint32_t src = e & 0xFFFFu;
-        const uint32_t g = s_delta[(e >> 16) & (B - 1)] + p;
-        kout[g] = s_k[src];
-        if constexpr (C::KV) vout[g] = s_v[src];
       }
     }
   }
+  return true;
 }
 
 // -------------------------------------------------------------- postscan
@@ -457,6 +468,7 @@ struct TileJob {
   uint32_t bias;             // subtracted from the scanned offsets (start of this multisplit in a shared scan)
   uint32_t prefetch_tile;    // a later tile of the same arrays to pull into L2 (>= num_tiles: none)
   Params bp;
+  uint32_t owner;            // which multisplit of a batch (tiles with one owner share bp)
 };
 
 // Postscan of one tile, run by a whole block:
@@ -470,9 +482,15 @@ struct TileJob {
 //  3. write, at each key's bucket-sorted in-tile position, its key or source index;
 //  4. walk the bucket-sorted order: out[delta[b] + p] = key (value), so every
 //     bucket's run is a contiguous, coalesced store.
-template <class C, class P>
-__device__ __forceinline__ void postscan_job(const TileJob<typename P::Params>& job, ScratchHeader* hdr,
-                                             unsigned char* smem) {
+//
+// PREPARE: fill the identifier's shared area first (false when the caller
+// prepared it for several tiles).  Returns false when the block must stop (a
+// bulk copy timed out or an offset was out of range; the error is recorded).
+// With `*bar_live` the caller learns whether the tile's mbarrier was
+// initialised (it must be invalidated before the next tile initialises it).
+template <class C, class P, bool PREPARE = true>
+__device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params>& job, ScratchHeader* hdr,
+                                             unsigned char* smem, bool* bar_live = nullptr) {
   using L = PostLayout<C, P>;
   constexpr uint32_t B = C::B;
   constexpr int LOGB = C::LOGB;
@@ -511,10 +529,13 @@ __device__ __forceinline__ void postscan_job(const TileJob<typename P::Params>& 
     s_k[i] = kin[base + i];
     if constexpr (C::KV) s_v[i] = vin[base + i];
   }
+  if (bar_live) *bar_live = bulk != 0;
   const uint32_t goff = (tid < B) ? job.offsets[tid * job.num_tiles + job.tile] - job.bias : 0u;
-  P::prepare(s_split, job.bp);
+  if constexpr (PREPARE) P::prepare(s_split, job.bp);
   if constexpr (LOGB > 5) {
-    for (uint32_t i = tid; i < C::WARPS * WB * C::WS; i += C::THREADS) s_wh[i] = 0u;
+    // the count table as 32-bit words (its byte size is a multiple of 4)
+    constexpr uint32_t WORDS = C::WARPS * WB * C::WS * sizeof(typename L::WhT) / 4;
+    for (uint32_t i = tid; i < WORDS; i += C::THREADS) s_wh[i] = 0u;
   }
   __syncthreads();
   if (bulk != 0) {
@@ -524,14 +545,38 @@ __device__ __forceinline__ void postscan_job(const TileJob<typename P::Params>& 
         record_error(hdr, DEV_ERR_BULK_COPY_TIMEOUT);
         mbar_wait_bounded(s_bar, 0);  // let a late copy land before the block moves on
       }
-      return;
+      return false;
     }
   }
 
   if (cnt == C::TILE)
-    postscan_tile<C, P, true>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
-  else
-    postscan_tile<C, P, false>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
+    return postscan_tile<C, P, true>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
+  return postscan_tile<C, P, false>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
+}
+
+// Persistent postscan over tiles first, first + stride, ... below last, for
+// identifiers with a shared area (RANGE): the area is prepared again only when
+// the tile's owner (multisplit of a batch) changes, and each tile pulls the
+// block's next tile into L2.
+template <class C, class P, class JobAt>
+__device__ __forceinline__ void postscan_run(uint32_t first, uint32_t last, uint32_t stride, JobAt job_at,
+                                             ScratchHeader* hdr, unsigned char* smem) {
+  using L = PostLayout<C, P>;
+  uint32_t* s_split = reinterpret_cast<uint32_t*>(smem + L::OFF_SPLIT);
+  uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
+  uint32_t prepared_for = ~0u;  // owner whose parameters the shared area holds
+  for (uint32_t t = first; t < last; t += stride) {
+    const TileJob<typename P::Params> job = job_at(t, last - t > stride ? t + stride : ~0u);
+    if (job.owner != prepared_for) {  // block-uniform: every thread reads the same job
+      P::prepare(s_split, job.bp);
+      prepared_for = job.owner;
+    }
+    bool bar_live = false;
+    const bool ok = postscan_job<C, P, false>(job, hdr, smem, &bar_live);
+    __syncthreads();  // shared buffers are reused by the next tile
+    if (!ok) return;
+    if (bar_live && threadIdx.x == 0) mbar_inval(s_bar);
+  }
 }
 
 // Plain postscan: one block per tile of one multisplit.
@@ -544,8 +589,26 @@ __global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P>::MIN_BLOCKS)) po
   const TileJob<typename P::Params> job{kin,        vin,     kout, vout,
                                         n,          num_tiles, blockIdx.x, offsets,
                                         0u,         prefetch_dist != 0 ? blockIdx.x + prefetch_dist : ~0u,
-                                        bp};
+                                        bp,         0u};
   postscan_job<C, P>(job, hdr, smem);
+}
+
+// Persistent plain postscan (identifiers with a shared area): block b runs
+// tiles b, b + grid, ...  Blocks that run at the same time then work on
+// neighbouring tiles, whose runs of one bucket are neighbours in the output,
+// so partly written sectors merge in L2 before they reach DRAM.
+template <class C, class P>
+__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P>::MIN_BLOCKS)) postscan_persistent_kernel(
+    const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
+    uint32_t* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
+    typename P::Params bp, ScratchHeader* hdr) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  postscan_run<C, P>(
+      blockIdx.x, num_tiles, gridDim.x,
+      [&](uint32_t t, uint32_t prefetch) {
+        return TileJob<typename P::Params>{kin, vin, kout, vout, n, num_tiles, t, offsets, 0u, prefetch, bp, 0u};
+      },
+      hdr, smem);
 }
 
 }  // namespace gms
