@@ -76,6 +76,9 @@ _PROTOS = {
     "gms_sort_scratch_bytes": [_U32, _I32, _I32, _PSZ],
     "gms_sort_key_only": [_P, _P, _U32, _I32, _P, _SZ, _P],
     "gms_sort_key_value": [_P, _P, _P, _P, _U32, _I32, _P, _SZ, _P],
+    "gms_sort_bits_scratch_bytes": [_U32, _I32, _I32, _I32, _I32, _PSZ],
+    "gms_sort_bits_key_only": [_P, _P, _U32, _I32, _I32, _I32, _P, _SZ, _P],
+    "gms_sort_bits_key_value": [_P, _P, _P, _P, _U32, _I32, _I32, _I32, _P, _SZ, _P],
     "gms_sort_7bit_scratch_bytes": [_U32, _I32, _PSZ],
     "gms_sort_7bit_key_only": [_P, _P, _U32, _P, _SZ, _P],
     "gms_sort_7bit_key_value": [_P, _P, _P, _P, _U32, _P, _SZ, _P],

@@ -389,6 +389,36 @@ for _bits in (4, 5, 6, 8):
     _define_sorts(_bits)
 
 
+def multisplit_sort_bits_allocate(n_elements, context, begin_bit=0, end_bit=32, digit_bits=8, pairs=False):
+    """Scratch for a stable sort by key bits [begin_bit, end_bit) (the begin/end
+    bit arguments of the CUB sorts the reference compares against,
+    src/main/main_bms.cu:199)."""
+    nbytes = ctypes.c_size_t()
+    check(_lib.load().gms_sort_bits_scratch_bytes(n_elements, begin_bit, end_bit, digit_bits, int(pairs),
+                                                  ctypes.byref(nbytes)), "multisplit_sort_bits_allocate")
+    context.temp_storage_bytes = nbytes.value
+    context.d_temp_storage = _alloc_scratch(max(nbytes.value, 256))
+    context.bit_range = (begin_bit, end_bit, digit_bits)
+
+
+def multisplit_sort_bits(d_key_in, d_key_out_ms, n_elements, context, stream=None):
+    """Stable sort of keys by the bit range given at allocation."""
+    b, e, d = context.bit_range
+    check(_lib.load().gms_sort_bits_key_only(_ptr(d_key_in), _ptr(d_key_out_ms), n_elements, b, e, d,
+                                             _scratch(context), context.temp_storage_bytes, _stream(stream)),
+          "multisplit_sort_bits")
+
+
+def multisplit_sort_bits_pairs(d_key_in, d_key_out_ms, d_value_in, d_value_out_ms, n_elements, context,
+                               stream=None):
+    """Stable sort of key-value pairs by the key bit range given at allocation."""
+    b, e, d = context.bit_range
+    check(_lib.load().gms_sort_bits_key_value(_ptr(d_key_in), _ptr(d_key_out_ms), _ptr(d_value_in),
+                                              _ptr(d_value_out_ms), n_elements, b, e, d, _scratch(context),
+                                              context.temp_storage_bytes, _stream(stream)),
+          "multisplit_sort_bits_pairs")
+
+
 # -------------------------------------------------------------- compaction
 
 

@@ -159,6 +159,20 @@ bool sort_schedule(int digit_bits, SortSchedule* s) {
   }
 }
 
+// Partial-key schedule: digits of digit_bits bits from begin_bit up to end_bit,
+// the last one narrower when the range is not a whole number of digits.
+bool bit_schedule(int begin_bit, int end_bit, int digit_bits, SortSchedule* s) {
+  if (digit_bits < 4 || digit_bits > 8 || begin_bit < 0 || end_bit > 32 || begin_bit > end_bit) return false;
+  s->passes = 0;
+  for (int sh = begin_bit; sh < end_bit; sh += digit_bits) {
+    const int w = end_bit - sh < digit_bits ? end_bit - sh : digit_bits;
+    s->shift[s->passes] = uint32_t(sh);
+    s->buckets[s->passes] = w == 1 ? 2u : (1u << w);
+    ++s->passes;
+  }
+  return true;
+}
+
 struct SortLayout {
   size_t ms_bytes;   // multisplit scratch (largest over the schedule's digit widths)
   size_t off_keys;   // ping-pong keys
@@ -169,6 +183,10 @@ struct SortLayout {
 SortLayout sort_layout(uint32_t n, bool kv, const SortSchedule& sch) {
   SortLayout L;
   L.ms_bytes = 0;
+  if (sch.passes == 0) {  // nothing to sort: the input is copied
+    L.off_keys = L.off_vals = L.bytes = 0;
+    return L;
+  }
   for (int p = 0; p < sch.passes; ++p) {
     int logb = 0;
     valid_buckets(sch.buckets[p], &logb);
@@ -185,15 +203,19 @@ SortLayout sort_layout(uint32_t n, bool kv, const SortSchedule& sch) {
 // ping-pong between the output and the scratch copy so the last pass lands in
 // the output (an odd number of passes starts in the output, an even one in the
 // copy), and the input is never written.
-gms_status sort_impl(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
-                     bool kv, int digit_bits, void* scratch, size_t scratch_bytes, cudaStream_t stream) {
-  SortSchedule sch;
-  if (!sort_schedule(digit_bits, &sch)) return GMS_ERROR_INVALID_VALUE;
+gms_status sort_run(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                    bool kv, const SortSchedule& sch, void* scratch, size_t scratch_bytes, cudaStream_t stream) {
   if (n == 0) return GMS_SUCCESS;
-  if (kin == nullptr || kout == nullptr || scratch == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (kin == nullptr || kout == nullptr || (scratch == nullptr && sch.passes > 0)) return GMS_ERROR_INVALID_VALUE;
   if (kv && (vin == nullptr || vout == nullptr)) return GMS_ERROR_INVALID_VALUE;
   const SortLayout L = sort_layout(n, kv, sch);
   if (scratch_bytes < L.bytes) return GMS_ERROR_SCRATCH_TOO_SMALL;
+  if (sch.passes == 0) {
+    if (overlaps(kin, kout, n) || (kv && overlaps(vin, vout, n))) return GMS_ERROR_INVALID_VALUE;
+    cudaError_t e = cudaMemcpyAsync(kout, kin, size_t(n) * 4, cudaMemcpyDeviceToDevice, stream);
+    if (e == cudaSuccess && kv) e = cudaMemcpyAsync(vout, vin, size_t(n) * 4, cudaMemcpyDeviceToDevice, stream);
+    return cuda_status(e);
+  }
   auto* base = static_cast<unsigned char*>(scratch);
   uint32_t* tk = reinterpret_cast<uint32_t*>(base + L.off_keys);
   uint32_t* tv = kv ? reinterpret_cast<uint32_t*>(base + L.off_vals) : nullptr;
@@ -214,6 +236,13 @@ gms_status sort_impl(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, u
     vi = vo;
   }
   return GMS_SUCCESS;
+}
+
+gms_status sort_impl(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                     bool kv, int digit_bits, void* scratch, size_t scratch_bytes, cudaStream_t stream) {
+  SortSchedule sch;
+  if (!sort_schedule(digit_bits, &sch)) return GMS_ERROR_INVALID_VALUE;
+  return sort_run(kin, kout, vin, vout, n, kv, sch, scratch, scratch_bytes, stream);
 }
 
 gms_status compaction_impl(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n,
@@ -384,6 +413,30 @@ gms_status gms_sort_key_value(const uint32_t* d_key_in, uint32_t* d_key_out, con
                               size_t scratch_bytes, gms_stream_t stream) {
   return sort_impl(d_key_in, d_key_out, d_value_in, d_value_out, n, true, digit_bits, d_scratch, scratch_bytes,
                    stream);
+}
+
+gms_status gms_sort_bits_scratch_bytes(uint32_t max_elements, int begin_bit, int end_bit, int digit_bits,
+                                      int key_value, size_t* bytes) {
+  SortSchedule sch;
+  if (bytes == nullptr || !bit_schedule(begin_bit, end_bit, digit_bits, &sch)) return GMS_ERROR_INVALID_VALUE;
+  *bytes = sort_layout(max_elements, key_value != 0, sch).bytes;
+  return GMS_SUCCESS;
+}
+
+gms_status gms_sort_bits_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n, int begin_bit,
+                                  int end_bit, int digit_bits, void* d_scratch, size_t scratch_bytes,
+                                  gms_stream_t stream) {
+  SortSchedule sch;
+  if (!bit_schedule(begin_bit, end_bit, digit_bits, &sch)) return GMS_ERROR_INVALID_VALUE;
+  return sort_run(d_key_in, d_key_out, nullptr, nullptr, n, false, sch, d_scratch, scratch_bytes, stream);
+}
+
+gms_status gms_sort_bits_key_value(const uint32_t* d_key_in, uint32_t* d_key_out, const uint32_t* d_value_in,
+                                   uint32_t* d_value_out, uint32_t n, int begin_bit, int end_bit, int digit_bits,
+                                   void* d_scratch, size_t scratch_bytes, gms_stream_t stream) {
+  SortSchedule sch;
+  if (!bit_schedule(begin_bit, end_bit, digit_bits, &sch)) return GMS_ERROR_INVALID_VALUE;
+  return sort_run(d_key_in, d_key_out, d_value_in, d_value_out, n, true, sch, d_scratch, scratch_bytes, stream);
 }
 
 gms_status gms_sort_7bit_scratch_bytes(uint32_t max_elements, int key_value, size_t* bytes) {

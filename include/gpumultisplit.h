@@ -173,6 +173,20 @@ gms_status gms_sort_key_value(const uint32_t* d_key_in, uint32_t* d_key_out, con
                               uint32_t* d_value_out, uint32_t n, int digit_bits, void* d_scratch,
                               size_t scratch_bytes, gms_stream_t stream);
 
+/* Partial-key sorts: a stable sort by key bits [begin_bit, end_bit), as the
+ * begin_bit / end_bit arguments of the CUB radix sorts the reference's drivers
+ * compare against (src/main/main_bms.cu:199).  Digits of digit_bits (4..8)
+ * bits from begin_bit, the last one narrower when the range is not a whole
+ * number of digits; begin_bit == end_bit copies the input. */
+gms_status gms_sort_bits_scratch_bytes(uint32_t max_elements, int begin_bit, int end_bit, int digit_bits,
+                                      int key_value, size_t* bytes);
+gms_status gms_sort_bits_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n, int begin_bit,
+                                  int end_bit, int digit_bits, void* d_scratch, size_t scratch_bytes,
+                                  gms_stream_t stream);
+gms_status gms_sort_bits_key_value(const uint32_t* d_key_in, uint32_t* d_key_out, const uint32_t* d_value_in,
+                                   uint32_t* d_value_out, uint32_t n, int begin_bit, int end_bit, int digit_bits,
+                                   void* d_scratch, size_t scratch_bytes, gms_stream_t stream);
+
 /* ----------------------------------------------------------- compaction */
 /* Replaces compaction_allocate_key_only / _key_value
  * (src/kernels/compaction/multisplit2_compaction.cuh:491-517). */

@@ -88,3 +88,32 @@ GMS_DROPIN_SORT(5)
 GMS_DROPIN_SORT(6)
 GMS_DROPIN_SORT(8)
 #undef GMS_DROPIN_SORT
+
+// Stable sort by key bits [begin_bit, end_bit) with digit_bits-wide digits (an
+// extension: the reference reaches partial-key sorts only through CUB,
+// src/main/main_bms.cu:199).
+inline void multisplit_sort_bits_allocate(uint32_t n_elements, ms_sort_context& context, int begin_bit, int end_bit,
+                                          int digit_bits, bool pairs) {
+  size_t bytes = 0;
+  gms_status st = gms_sort_bits_scratch_bytes(n_elements, begin_bit, end_bit, digit_bits, pairs ? 1 : 0, &bytes);
+  if (bytes < 256) bytes = 256;
+  if (st == GMS_SUCCESS && cudaMalloc(&context.d_temp_storage, bytes) != cudaSuccess) st = GMS_ERROR_CUDA;
+  gms::last_status() = st;
+  if (st != GMS_SUCCESS) return;
+  context.temp_storage_bytes = bytes;
+  context.d_histogram = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(context.d_temp_storage) + 256);
+}
+
+inline void multisplit_sort_bits(uint32_t* d_key_in, uint32_t* d_key_out_ms, uint32_t n_elements,
+                                 ms_sort_context& context, int begin_bit, int end_bit, int digit_bits) {
+  gms::last_status() = gms_sort_bits_key_only(d_key_in, d_key_out_ms, n_elements, begin_bit, end_bit, digit_bits,
+                                              context.d_temp_storage, context.temp_storage_bytes, 0);
+}
+
+inline void multisplit_sort_bits_pairs(uint32_t* d_key_in, uint32_t* d_key_out_ms, uint32_t* d_value_in,
+                                       uint32_t* d_value_out_ms, uint32_t n_elements, ms_sort_context& context,
+                                       int begin_bit, int end_bit, int digit_bits) {
+  gms::last_status() =
+      gms_sort_bits_key_value(d_key_in, d_key_out_ms, d_value_in, d_value_out_ms, n_elements, begin_bit, end_bit,
+                              digit_bits, context.d_temp_storage, context.temp_storage_bytes, 0);
+}

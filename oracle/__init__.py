@@ -6,7 +6,8 @@ calls it.
 
   liboracle.so   plain-C restatement of the reference's CPU multisplit
                  (src/cpu_functions.h:155-288) plus histogram, tile counts,
-                 7-bit sort schedule and compaction (oracle.c cites each).
+                 the sort digit schedules, partial-key sorts and compaction
+                 (oracle.c cites each).
   libgms_ref.so  the reference's OWN cpu_multisplit_general /
                  cpu_multisplit_pairs_general compiled from its sources
                  (ref_shim.cpp, `make ref`); built only where the reference
@@ -171,6 +172,22 @@ def sort(keys, values=None, digit_bits: int = 7):
 
 def sort_7bit(keys, values=None):
     return sort(keys, values, 7)
+
+
+def sort_bits(keys, values=None, begin_bit: int = 0, end_bit: int = 32, digit_bits: int = 8):
+    """Stable sort by key bits [begin_bit, end_bit) in digit_bits-wide multisplit passes."""
+    keys = _u32(keys)
+    n = keys.size
+    kout, tk = np.empty(n, np.uint32), np.empty(n, np.uint32)
+    vout = tv = None
+    if values is not None:
+        values = _u32(values)
+        vout, tv = np.empty(n, np.uint32), np.empty(n, np.uint32)
+    rc = lib().oracle_sort_bits(_p(keys), _p(kout), _p(values), _p(vout), ctypes.c_uint32(n), _p(tk), _p(tv),
+                                ctypes.c_int(begin_bit), ctypes.c_int(end_bit), ctypes.c_int(digit_bits))
+    if rc != 0:
+        raise ValueError("invalid bit range or digit width")
+    return kout, vout
 
 
 def compaction(keys, d: Desc, values=None):

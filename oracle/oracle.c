@@ -154,6 +154,39 @@ int oracle_sort(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32
   return 0;
 }
 
+/* Stable sort by key bits [begin_bit, end_bit): multisplits on digits of
+ * digit_bits bits from begin_bit, the last one narrower (the partial-key form
+ * of the CUB radix sorts the reference's drivers use, src/main/main_bms.cu:199).
+ * begin_bit == end_bit copies.  Returns 0, or -1 for an invalid range. */
+int oracle_sort_bits(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                     uint32_t* tmp_k, uint32_t* tmp_v, int begin_bit, int end_bit, int digit_bits) {
+  if (digit_bits < 4 || digit_bits > 8 || begin_bit < 0 || end_bit > 32 || begin_bit > end_bit) return -1;
+  const int P = (end_bit - begin_bit + digit_bits - 1) / digit_bits;
+  if (P == 0) {
+    memcpy(kout, kin, sizeof(uint32_t) * n);
+    if (vin) memcpy(vout, vin, sizeof(uint32_t) * n);
+    return 0;
+  }
+  const uint32_t* src_k = kin;
+  const uint32_t* src_v = vin;
+  for (int p = 0; p < P; ++p) {
+    const int shift = begin_bit + p * digit_bits;
+    const int w = end_bit - shift < digit_bits ? end_bit - shift : digit_bits;
+    const int to_out = ((P - 1 - p) % 2) == 0;
+    uint32_t* dk = to_out ? kout : tmp_k;
+    uint32_t* dv = to_out ? vout : tmp_v;
+    oracle_desc d;
+    memset(&d, 0, sizeof(d));
+    d.kind = ORACLE_BITS;
+    d.num_buckets = 1u << w;
+    d.shift = (uint32_t)shift;
+    multisplit(src_k, dk, vin ? src_v : NULL, vin ? dv : NULL, n, &d, NULL);
+    src_k = dk;
+    src_v = dv;
+  }
+  return 0;
+}
+
 void oracle_sort_7bit(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
                       uint32_t* tmp_k, uint32_t* tmp_v) {
   oracle_sort(kin, kout, vin, vout, n, tmp_k, tmp_v, 7);

@@ -37,6 +37,8 @@ void oracle_tile_counts(const uint32_t* kin, uint32_t n, const oracle_desc* d, u
 void oracle_histogram(const uint32_t* kin, uint32_t n, const oracle_desc* d, int32_t* hist);
 int oracle_sort(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
                 uint32_t* tmp_k, uint32_t* tmp_v, int digit_bits);
+int oracle_sort_bits(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
+                     uint32_t* tmp_k, uint32_t* tmp_v, int begin_bit, int end_bit, int digit_bits);
 void oracle_sort_7bit(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
                       uint32_t* tmp_k, uint32_t* tmp_v);
 uint32_t oracle_compaction(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,

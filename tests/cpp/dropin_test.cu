@@ -161,6 +161,33 @@ static void test_sort(uint32_t n, bool and4, SortFns fns = SORT_FNS(7)) {
   printf("sort %d-bit n=%u %s\n", fns.bits, n, and4 ? "and4" : "uniform");
 }
 
+static void test_sort_bits(uint32_t n, int begin, int end, int digit) {
+  std::vector<uint32_t> k(n), v(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    k[i] = next_u32();
+    v[i] = i;
+  }
+  const uint32_t mask = end - begin >= 32 ? 0xFFFFFFFFu : ((1u << (end - begin)) - 1u);
+  std::vector<uint32_t> idx(n);
+  std::iota(idx.begin(), idx.end(), 0u);
+  std::stable_sort(idx.begin(), idx.end(),
+                   [&](uint32_t a, uint32_t b) { return ((k[a] >> begin) & mask) < ((k[b] >> begin) & mask); });
+  std::vector<uint32_t> rk(n);
+  for (uint32_t i = 0; i < n; ++i) rk[i] = k[idx[i]];
+  DeviceArrays d(n);
+  cudaMemcpy(d.k, k.data(), 4 * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(d.v, v.data(), 4 * n, cudaMemcpyHostToDevice);
+  ms_sort_context ctx;
+  multisplit_sort_bits_allocate(n, ctx, begin, end, digit, true);
+  multisplit_sort_bits_pairs(d.k, d.ko, d.v, d.vo, n, ctx, begin, end, digit);
+  cudaDeviceSynchronize();
+  CHECK(multisplit_last_error() == GMS_SUCCESS, "partial-key sort");
+  CHECK(download(d.ko, n) == rk, "partial-key sort keys");
+  CHECK(download(d.vo, n) == idx, "partial-key sort values (stable)");
+  multisplit_sort_release_memory(ctx);
+  printf("sort bits [%d,%d) by %d-bit digits n=%u\n", begin, end, digit, n);
+}
+
 template <class F>
 static void test_compaction(const char* name, uint32_t n, F f) {
   std::vector<uint32_t> k(n), v(n);
@@ -223,6 +250,8 @@ int main() {
   test_sort(50002, true, SORT_FNS(5));
   test_sort(50003, false, SORT_FNS(6));
   test_sort(50004, false, SORT_FNS(8));
+  test_sort_bits(70001, 3, 17, 5);
+  test_sort_bits(4096, 0, 32, 8);
   test_compaction("test_bucket<1> (key & 1)", 100001, test_bucket<1, uint32_t>());
   test_compaction("gms::mask_bucket{1}", 4096, gms::mask_bucket{1});
   test_histogram("gms::delta_bucket", 1 << 20, 256, gms::delta_bucket{256});

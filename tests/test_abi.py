@@ -123,6 +123,20 @@ def test_sort_scratch_all_digit_widths(gms_lib):
         assert gms_lib.gms_sort_scratch_bytes(100, bad, 0, ctypes.byref(sb)) == _lib.GMS_ERROR_INVALID_VALUE
 
 
+def test_partial_key_sort_scratch_and_checks(gms_lib):
+    sb = ctypes.c_size_t()
+    for begin, end, digit, widths in ((0, 32, 8, (256,)), (3, 17, 5, (32, 16)), (20, 21, 6, (2,))):
+        assert gms_lib.gms_sort_bits_scratch_bytes(1 << 20, begin, end, digit, 1, ctypes.byref(sb)) == 0
+        need = max(scratch_bytes(1 << 20, b, 1)[1] for b in widths) + 8 * (1 << 20)
+        assert sb.value >= need
+    assert gms_lib.gms_sort_bits_scratch_bytes(100, 9, 9, 8, 0, ctypes.byref(sb)) == 0 and sb.value == 0
+    for begin, end, digit in ((5, 4, 8), (0, 33, 8), (-1, 8, 8), (0, 8, 3), (0, 8, 9)):
+        assert gms_lib.gms_sort_bits_scratch_bytes(100, begin, end, digit, 0, ctypes.byref(sb)) == \
+            _lib.GMS_ERROR_INVALID_VALUE
+        assert gms_lib.gms_sort_bits_key_only(1 << 20, 2 << 20, 10, begin, end, digit, 1 << 24, 1 << 20, None) == \
+            _lib.GMS_ERROR_INVALID_VALUE
+
+
 def test_tuning_table_host_logic(gms_lib):
     """Tile variants, the built-in table, set/get/reset and their checks (host only)."""
     from gpumultisplit_gb300 import batched

@@ -71,6 +71,31 @@ def test_sort_other_widths(gms_lib, oracle_mod, bits, n):
     np.testing.assert_array_equal(gv, rv)
 
 
+@pytest.mark.parametrize("begin,end,digit", [(0, 32, 8), (0, 8, 4), (3, 17, 5), (20, 21, 6), (9, 9, 7),
+                                              (12, 32, 7)])
+@pytest.mark.parametrize("n", [0, 1, 4097, 300007])
+def test_partial_key_sort(gms_lib, oracle_mod, begin, end, digit, n):
+    """Stable sort by key bits [begin, end) (the CUB begin/end-bit form)."""
+    keys = datagen.as_u32(datagen.uniform_u32(n, 500 + n + begin))
+    vals = np.arange(n, dtype=np.uint32)
+    rk, rv = oracle_mod.sort_bits(keys, vals, begin, end, digit)
+    dk, ok = to_dev(keys), to_dev(np.zeros(n, np.uint32))
+    dv, ov = to_dev(vals), to_dev(np.zeros(n, np.uint32))
+    ctx = gms.ms_sort_context()
+    gms.multisplit_sort_bits_allocate(n, ctx, begin, end, digit, pairs=True)
+    gms.multisplit_sort_bits_pairs(dk, ok, dv, ov, n, ctx)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(host(ok), rk)
+    np.testing.assert_array_equal(host(ov), rv)
+    ok2 = to_dev(np.zeros(n, np.uint32))
+    ctx2 = gms.ms_sort_context()
+    gms.multisplit_sort_bits_allocate(n, ctx2, begin, end, digit)
+    gms.multisplit_sort_bits(dk, ok2, n, ctx2)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(host(ok2), rk)
+    np.testing.assert_array_equal(host(dk), keys)
+
+
 def test_sort7_golden(gms_lib, golden):
     from test_oracle_golden import gen_keys, sha
 

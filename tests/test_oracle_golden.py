@@ -139,3 +139,17 @@ def test_oracle_matches_reference_code(oracle_mod):
         ko, vo, _ = o.multisplit(keys, d, vals)
         rk, rv = o.ref_multisplit(keys, d, vals)
         assert np.array_equal(ko, rk) and np.array_equal(vo, rv), (trial, kind, B, n)
+
+
+@pytest.mark.parametrize("begin,end,digit", [(0, 32, 8), (0, 8, 4), (3, 17, 5), (20, 21, 6), (9, 9, 7), (12, 32, 7)])
+def test_partial_key_sort_oracle(oracle_mod, begin, end, digit):
+    """Stable sort by bits [begin, end) equals numpy's stable argsort on those bits."""
+    keys = datagen.as_u32(datagen.uniform_u32(30011, 77))
+    vals = np.arange(keys.size, dtype=np.uint32)
+    ko, vo = oracle_mod.sort_bits(keys, vals, begin, end, digit)
+    field = (keys.astype(np.uint64) >> begin) & ((1 << (end - begin)) - 1)
+    order = np.argsort(field, kind="stable")
+    assert np.array_equal(vo, order.astype(np.uint32))
+    assert np.array_equal(ko, keys[order])
+    with pytest.raises(ValueError):
+        oracle_mod.sort_bits(keys, vals, 5, 4, 8)
