@@ -71,10 +71,11 @@ struct KeyCounter {
   static constexpr uint32_t R = B >= 32 ? 1u : 32u / B;  // histogram replicas (atomic path)
   static constexpr uint32_t HIST_WORDS = B * R;         // >= 32
   Id ident;
-  uint32_t* s_hist;                      // HIST_WORDS (atomic path) or WARPS*32 (ballot path)
+  uint32_t* s_hist;                      // 2 x HIST_WORDS (atomic path) or WARPS*32 (ballot path)
   uint32_t acc[4] = {0u, 0u, 0u, 0u};    // ballot path: independent accumulators keep the chains parallel
   uint32_t xm[kBallot ? LOGB : 1];
   uint32_t slot;                          // atomic path: this lane's replica offset
+  uint32_t buf = 0;                       // atomic path: histogram being filled (0 or HIST_WORDS)
 
   __device__ __forceinline__ KeyCounter(const Id& id, uint32_t* hist) : ident(id), s_hist(hist) {
     const uint32_t lane = lane_id();
@@ -95,22 +96,27 @@ struct KeyCounter {
       for (int i = 0; i < LOGB; ++i) m &= __ballot_sync(~0u, (b >> i) & 1u) ^ xm[i];
       acc[A] += __popc(m);
     } else {
-      if (valid) atomicAdd(&s_hist[b * R + slot], 1u);
+      if (valid) atomicAdd(&s_hist[buf + b * R + slot], 1u);
     }
   }
 
-  // Shared words the counter needs for a block of `warps` warps.
-  __host__ __device__ static constexpr uint32_t smem_words(int warps) { return kBallot ? uint32_t(warps) * 32u : HIST_WORDS; }
+  // Shared words the counter needs for a block of `warps` warps.  The atomic
+  // path keeps two histograms: one tile is read out and cleared while the
+  // next one is counted into the other, so a tile needs one barrier.
+  __host__ __device__ static constexpr uint32_t smem_words(int warps) {
+    return kBallot ? uint32_t(warps) * 32u : 2u * HIST_WORDS;
+  }
 
-  // Zero the shared histogram (atomic path); all threads call, a barrier must follow.
+  // Zero the shared histograms (atomic path); all threads call, a barrier must follow.
   __device__ __forceinline__ void clear_shared() {
     if constexpr (!kBallot) {
-      for (uint32_t i = threadIdx.x; i < HIST_WORDS; i += blockDim.x) s_hist[i] = 0u;
+      for (uint32_t i = threadIdx.x; i < 2u * HIST_WORDS; i += blockDim.x) s_hist[i] = 0u;
     }
   }
 
-  // Block totals: after the call (which contains barriers), thread b < B returns
-  // the block's count of bucket b, and the counter is reset for the next tile.
+  // Block totals: after the call (which contains a barrier), thread b < B
+  // returns the block's count of bucket b, and the counter is ready for the
+  // next tile.
   __device__ __forceinline__ uint32_t block_total() {
     const uint32_t tid = threadIdx.x;
     uint32_t total = 0;
@@ -124,15 +130,17 @@ struct KeyCounter {
       }
       __syncthreads();
     } else {
+      // The barrier ends this tile's counting; the histogram is cleared here
+      // and filled again two tiles later, after the next tile's barrier.
       __syncthreads();
       if (tid < B) {
 #pragma unroll
         for (uint32_t r = 0; r < R; ++r) {
-          total += s_hist[tid * R + r];
-          s_hist[tid * R + r] = 0u;
+          total += s_hist[buf + tid * R + r];
+          s_hist[buf + tid * R + r] = 0u;
         }
       }
-      __syncthreads();
+      buf ^= HIST_WORDS;
     }
     return total;
   }
