@@ -10,6 +10,7 @@ import os
 import shutil
 import subprocess
 import sys
+import tempfile
 from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
@@ -84,8 +85,16 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     if not force and not needs_build():
         return LIB_PATH
     nvcc = nvcc_path()
-    obj_dir = LIB_DIR / "obj"
-    obj_dir.mkdir(parents=True, exist_ok=True)
+    LIB_DIR.mkdir(parents=True, exist_ok=True)
+    stale = LIB_DIR / "obj"  # objects of earlier builds, which kept them next to the library
+    if stale.is_dir():
+        shutil.rmtree(stale)
+    with tempfile.TemporaryDirectory(prefix="gms_build_") as tmp_dir:
+        _compile_and_link(nvcc, Path(tmp_dir), verbose, extra_flags)
+    return LIB_PATH
+
+
+def _compile_and_link(nvcc: str, obj_dir: Path, verbose: bool, extra_flags: list[str] | None) -> None:
     flags = ARCH_FLAGS + NVCC_FLAGS + list(extra_flags or [])
     units = _units()
     # Largest units first so the parallel build ends sooner.
@@ -100,7 +109,6 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     tmp = LIB_DIR / (LIB_PATH.name + ".tmp")
     _run([nvcc, *ARCH_FLAGS, "-shared", "-o", str(tmp), *map(str, objs)], verbose)
     os.replace(tmp, LIB_PATH)
-    return LIB_PATH
 
 
 if __name__ == "__main__":
