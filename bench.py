@@ -416,9 +416,12 @@ def run_sweep(a, dev):
                 gms.multisplit_sort_release_memory(ctx)
 
 
-def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: float = 64.0, verify: int = 24):
+def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: float = 64.0, verify: int = 24,
+                verify_all: bool = True):
     """Serving form under Poisson arrivals against the plain per-request calls on
-    the same trace: p50/p99 latency (arrival to result) and Gkeys/s."""
+    the same trace: p50/p99 latency (arrival to result) and Gkeys/s.  With
+    verify_all, every request of the trace is then served once more (untimed)
+    and each result is compared with the plain call on the same input."""
     import torch
 
     import gpumultisplit_gb300 as gms
@@ -520,6 +523,53 @@ def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: floa
     for i in kept:
         server.release(ids[i])
     server.close()
+    kept.clear()
+    del server
+
+    # ---- every request, untimed: served result == plain call, bit for bit
+    verified_all = None
+    if verify_all:
+        server = gms.Server(arena_bytes=int(arena_gb * (1 << 30)))
+        h = server._h
+        index = {}
+        for i in range(m):
+            st = lib.gms_server_submit(h, ctypes.byref(reqs[i]), ctypes.byref(rid))
+            if st != 0:
+                raise RuntimeError(f"submit failed: {st}")
+            index[rid.value] = i
+            server._meta[rid.value] = (names[ops[i]], int(sizes[i]), reqs[i].d_value_in is not None,
+                                       desc_for(i)[1], None)
+        vctx = {}
+        vk = torch.empty(16 << 20, dtype=torch.int32, device=dev)
+        vv = torch.empty(16 << 20, dtype=torch.int32, device=dev)
+        vh = torch.empty(256, dtype=torch.int32, device=dev)
+        checked, bad = 0, 0
+        while checked < m:
+            done_ids = server.take_completed()
+            if not done_ids:
+                time.sleep(2e-4)
+                continue
+            for r in done_ids:
+                i = index[r]
+                lib.gms_server_poll(h, r, ctypes.byref(res))
+                got = server._result(r, res)
+                op, n = names[ops[i]], int(sizes[i])
+                kin = keys_pool[offs[i]:offs[i] + n]
+                vin = vals_pool[offs[i]:offs[i] + n] if reqs[i].d_value_in else None
+                ident = gms.test_bucket(1) if op == "compaction" else gms.delta_bucket()
+                ref = _plain_request(gms, op, kin, vin, n, desc_for(i)[1], ident, vctx, vk, vv, vh)
+                if op == "histogram":
+                    same = bool(torch.equal(got.histogram, ref[0]))
+                else:
+                    same = bool(torch.equal(got.keys, ref[0])) and (vin is None or bool(torch.equal(got.values, ref[1])))
+                    if op == "compaction":
+                        same &= got.num_bucket0 == ref[2]
+                bad += 0 if (same and res.status == 0) else 1
+                server.release(r)
+                checked += 1
+        server.close()
+        del server, vk, vv, vh, vctx
+        verified_all = bad == 0
 
     # ---- plain per-request calls on the same trace (one stream, in arrival order)
     plain_lat = np.zeros(m)
@@ -559,8 +609,8 @@ def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: floa
         "max_requests_in_round": int(stats["max_requests_in_round"]),
         "launches": int(stats["launches"]),
         "arena_peak_gb": stats["arena_peak_bytes"] / (1 << 30),
-        "verified_identical": bool(ok),
-        "verified_requests": len(kept),
+        "verified_identical": bool(ok) and verified_all is not False,
+        "verified_requests": m if verify_all else len(kept),
     }
 
 
