@@ -21,9 +21,8 @@ enum DeviceError : uint32_t {
 struct ScratchHeader {
   uint32_t error;       // first DeviceError recorded in the current call
   uint32_t error_info;  // block that recorded it
-  uint32_t ticket;      // scan chunk / one-pass tile ticket counter
-  uint32_t done;        // blocks of the one-pass histogram that have finished
-  uint32_t reserved[60];
+  uint32_t ticket;      // scan chunk ticket counter
+  uint32_t reserved[61];
 };
 static_assert(sizeof(ScratchHeader) == 256, "header is 256 bytes");
 
@@ -118,16 +117,6 @@ __device__ __forceinline__ void st_relaxed_u64(uint64_t* p, uint64_t v) {
 __device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t* p) {
   uint64_t v;
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
-  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
-  uint32_t v;
-  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
 

@@ -34,12 +34,6 @@ inline cudaError_t ensure_smem_limit(Kernel k, size_t bytes, std::atomic<uint64_
 #define GMS_PREFETCH_WAVES 2
 #endif
 
-// One-call multisplits use the one-pass form (histogram, then a postscan with
-// decoupled look-back) when 1; 0 keeps prescan, scan and postscan.
-#ifndef GMS_ONE_PASS
-#define GMS_ONE_PASS 1
-#endif
-
 template <class Kernel>
 inline uint32_t persistent_grid(Kernel k, int threads, uint32_t work, std::atomic<int>& per_sm_cache,
                                 size_t smem = 0) {
@@ -67,35 +61,6 @@ cudaError_t launch_multisplit(const uint32_t* kin, const uint32_t* vin, uint32_t
   auto* hdr = reinterpret_cast<ScratchHeader*>(scratch);
   auto* status = reinterpret_cast<uint64_t*>(scratch + g.off_status);
   auto* matrix = reinterpret_cast<uint32_t*>(scratch + g.off_matrix);
-
-  if (stages == STAGE_ALL && GMS_ONE_PASS && !P::USES_SMEM && n <= kOnePassMaxN) {
-    // One pass over the tiles: bucket counts and starts first, then the
-    // postscan resolves each tile's offsets by look-back (no count matrix).
-    auto* hist = reinterpret_cast<uint32_t*>(scratch + g.off_hist);
-    auto* starts = reinterpret_cast<uint32_t*>(scratch + g.off_starts);
-    auto* lookback = reinterpret_cast<uint32_t*>(scratch + g.off_lookback);
-    cudaError_t e = cudaMemsetAsync(scratch, 0, g.off_lookback + size_t(g.m) * 4, stream);
-    if (e != cudaSuccess) return e;
-    {
-      static std::atomic<int> per_sm{0};
-      auto kern = onepass_histogram_kernel<LOGB, P>;
-      const uint32_t grid = persistent_grid(kern, HIST_THREADS, (n + HIST_CHUNK - 1) / HIST_CHUNK, per_sm);
-      kern<<<grid, HIST_THREADS, 0, stream>>>(kin, n, hist, starts, hdr, params);
-      e = cudaGetLastError();
-      if (e != cudaSuccess) return e;
-    }
-    static std::atomic<uint64_t> smem_done{0};
-    static std::atomic<int> per_sm{0};
-    auto kern = onepass_postscan_kernel<C, P>;
-    constexpr size_t smem = PostLayout<C, P>::BYTES;
-    e = ensure_smem_limit(kern, smem, smem_done);
-    if (e != cudaSuccess) return e;
-    const uint32_t wave = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
-    const uint32_t dist = (GMS_PREFETCH_WAVES * wave) / 4u;
-    kern<<<g.num_tiles, C::THREADS, smem, stream>>>(kin, vin, kout, vout, n, g.num_tiles, starts, lookback, params,
-                                                      hdr, dist);
-    return cudaGetLastError();
-  }
 
   if (stages & STAGE_PRESCAN) {
     static std::atomic<int> per_sm{0};

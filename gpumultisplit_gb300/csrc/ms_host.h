@@ -54,12 +54,8 @@ constexpr uint32_t kScanChunk = 4096;  // SCAN_CHUNK in scan_kernels.cuh
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-// Scratch layout of one multisplit, in one of two forms:
-//   three-pass: [header 256 B][count matrix u32 x B*tiles][scan status u64 x chunks]
-//               (the matrix always starts at byte 256, whatever n is);
-//   one-pass:   [header 256 B][bucket counts u32 x B][bucket starts u32 x B]
-//               [look-back words u32 x B*tiles].
-// The scratch size covers both.
+// Scratch layout of one multisplit: [header 256 B][count matrix u32 x B*tiles][scan status u64 x chunks].
+// The matrix always starts at byte 256, whatever n is.
 struct Geometry {
   uint32_t tile = 0;
   uint32_t num_tiles = 0;
@@ -67,9 +63,6 @@ struct Geometry {
   uint32_t num_chunks = 0;  // scan chunks
   size_t off_status = 0;
   size_t off_matrix = 0;
-  size_t off_hist = 0;      // one-pass form
-  size_t off_starts = 0;
-  size_t off_lookback = 0;
   size_t bytes = 0;
 };
 
@@ -81,17 +74,9 @@ inline Geometry make_geometry(uint32_t n, int logb, bool kv) {
   g.num_chunks = (g.m + kScanChunk - 1) / kScanChunk;
   g.off_matrix = sizeof(ScratchHeader);
   g.off_status = align_up(g.off_matrix + size_t(g.m) * 4, 256);
-  const size_t three_pass = align_up(g.off_status + size_t(g.num_chunks) * 8, 256);
-  g.off_hist = sizeof(ScratchHeader);
-  g.off_starts = g.off_hist + (size_t(4) << logb);
-  g.off_lookback = align_up(g.off_starts + (size_t(4) << logb), 256);
-  const size_t one_pass = align_up(g.off_lookback + size_t(g.m) * 4, 256);
-  g.bytes = three_pass > one_pass ? three_pass : one_pass;
+  g.bytes = align_up(g.off_status + size_t(g.num_chunks) * 8, 256);
   return g;
 }
-
-// The one-pass form packs counts into 30 bits.
-constexpr uint32_t kOnePassMaxN = (1u << 30) - 1u;
 
 enum Stage : int { STAGE_PRESCAN = 1, STAGE_SCAN = 2, STAGE_POSTSCAN = 4, STAGE_ALL = 7 };
 

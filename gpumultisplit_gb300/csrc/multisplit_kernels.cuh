@@ -282,12 +282,10 @@ __device__ __forceinline__ uint32_t peers_by_ballot(uint32_t b) {
 }
 
 // Phases 1-4 of the postscan for one staged tile.  FULL: the tile holds
-// exactly TILE keys, so no per-key validity test is needed.  goff_of(total),
-// called by thread b < B once the tile's count `total` of bucket b is known,
-// returns the global output offset of the tile's bucket-b run.
-template <class C, class P, bool FULL, class GoffFn>
+// exactly TILE keys, so no per-key validity test is needed.
+template <class C, class P, bool FULL>
 __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
-                                              uint32_t cnt, GoffFn goff_of, const typename P::Params& bp,
+                                              uint32_t cnt, uint32_t goff, const typename P::Params& bp,
                                               ScratchHeader* hdr, unsigned char* smem) {
   using L = PostLayout<C, P>;
   using WhT = typename L::WhT;
@@ -382,7 +380,7 @@ __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint3
   // cause a store outside the output).  Thread b owns bucket b; the bucket
   // starts come from a block-wide exclusive scan (warp scans + warp totals).
   {
-    uint32_t total = 0, goff = 0;
+    uint32_t total = 0;
     if (tid < B) {
 #pragma unroll
       for (int w = 0; w < C::WARPS; ++w) {
@@ -391,7 +389,6 @@ __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint3
         *c_ptr = WhT(total);
         total += c;
       }
-      goff = goff_of(total);
       if (uint64_t(goff) + total > n) atomicOr(s_flag, 1u);
     }
     uint32_t incl = total;
@@ -480,58 +477,7 @@ struct TileJob {
   uint32_t prefetch_tile;    // a later tile of the same arrays to pull into L2 (>= num_tiles: none)
   Params bp;
   uint32_t owner;            // which multisplit of a batch (tiles with one owner share bp)
-  uint32_t* lb_status;       // one-pass form: look-back words, B per tile, tile-major
-  const uint32_t* lb_starts; // one-pass form: global start of every bucket
 };
-
-// Look-back words of the one-pass postscan: flag in bits 31..30 (0 = not yet
-// published, 1 = this tile's count only, 2 = inclusive count of all tiles up
-// to this one), count in bits 29..0 (the one-pass form needs n < 2^30).
-constexpr uint32_t LB_AGGREGATE = 1u << 30;
-constexpr uint32_t LB_INCLUSIVE = 2u << 30;
-constexpr uint32_t LB_VALUE_MASK = (1u << 30) - 1u;
-
-// Decoupled look-back for bucket b of tile t (thread b): publish this tile's
-// count, add predecessors' counts going back until one has published its
-// inclusive count, publish this tile's inclusive count, and return the global
-// offset of the tile's bucket-b run.  Tiles are numbered in ticket order, so
-// every predecessor is already running and publishes without waiting on this
-// one; each wait is still bounded, and a timeout records an error, sets *fail
-// and lets the tile publish so that its successors do not wait on it.
-template <uint32_t B, class Params>
-__device__ __forceinline__ uint32_t lookback_offset(const TileJob<Params>& job, uint32_t b, uint32_t total,
-                                                    ScratchHeader* hdr, uint32_t* fail) {
-  uint32_t* st = job.lb_status;
-  const size_t me = size_t(job.tile) * B + b;
-  if (job.tile == 0) {
-    st_relaxed_u32(&st[me], LB_INCLUSIVE | total);
-    return job.lb_starts[b];
-  }
-  st_relaxed_u32(&st[me], LB_AGGREGATE | total);
-  uint32_t prefix = 0;
-  uint32_t k = job.tile - 1;
-  uint64_t t0 = 0;
-  while (true) {
-    const uint32_t w = ld_relaxed_u32(&st[size_t(k) * B + b]);
-    const uint32_t flag = w >> 30;
-    if (flag == 0u) {
-      if (t0 == 0) {
-        t0 = global_timer_ns();
-      } else if (global_timer_ns() - t0 > kWaitLimitNs || error_recorded(hdr)) {
-        record_error(hdr, DEV_ERR_LOOKBACK_TIMEOUT);
-        atomicOr(fail, 1u);
-        break;
-      }
-      __nanosleep(20);
-      continue;
-    }
-    prefix += w & LB_VALUE_MASK;
-    if (flag == 2u || k == 0) break;
-    --k;
-  }
-  st_relaxed_u32(&st[me], LB_INCLUSIVE | ((prefix + total) & LB_VALUE_MASK));
-  return job.lb_starts[b] + prefix;
-}
 
 // Postscan of one tile, run by a whole block:
 //  0. bulk-copy the tile's keys (and values) into shared memory, prefetch the
@@ -550,10 +496,7 @@ __device__ __forceinline__ uint32_t lookback_offset(const TileJob<Params>& job, 
 // bulk copy timed out or an offset was out of range; the error is recorded).
 // With `*bar_live` the caller learns whether the tile's mbarrier was
 // initialised (it must be invalidated before the next tile initialises it).
-//
-// LOOKBACK: the one-pass form, where each bucket's offset comes from the
-// decoupled look-back over earlier tiles instead of a scanned count matrix.
-template <class C, class P, bool PREPARE = true, bool LOOKBACK = false>
+template <class C, class P, bool PREPARE = true>
 __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params>& job, ScratchHeader* hdr,
                                              unsigned char* smem, bool* bar_live = nullptr) {
   using L = PostLayout<C, P>;
@@ -595,8 +538,7 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params>& 
     if constexpr (C::KV) s_v[i] = vin[base + i];
   }
   if (bar_live) *bar_live = bulk != 0;
-  uint32_t goff = 0;
-  if constexpr (!LOOKBACK) goff = (tid < B) ? job.offsets[tid * job.num_tiles + job.tile] - job.bias : 0u;
+  const uint32_t goff = (tid < B) ? job.offsets[tid * job.num_tiles + job.tile] - job.bias : 0u;
   if constexpr (PREPARE) P::prepare(s_split, job.bp);
   if constexpr (LOGB > 5) {
     // the count table as 32-bit words (its byte size is a multiple of 4)
@@ -615,16 +557,9 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params>& 
     }
   }
 
-  if constexpr (LOOKBACK) {
-    uint32_t* s_flag = reinterpret_cast<uint32_t*>(smem + L::OFF_FLAG);
-    auto goff_of = [&](uint32_t total) { return lookback_offset<B>(job, tid, total, hdr, s_flag); };
-    if (cnt == C::TILE) return postscan_tile<C, P, true>(job.kout, job.vout, job.n, cnt, goff_of, job.bp, hdr, smem);
-    return postscan_tile<C, P, false>(job.kout, job.vout, job.n, cnt, goff_of, job.bp, hdr, smem);
-  } else {
-    auto goff_of = [goff](uint32_t) { return goff; };
-    if (cnt == C::TILE) return postscan_tile<C, P, true>(job.kout, job.vout, job.n, cnt, goff_of, job.bp, hdr, smem);
-    return postscan_tile<C, P, false>(job.kout, job.vout, job.n, cnt, goff_of, job.bp, hdr, smem);
-  }
+  if (cnt == C::TILE)
+    return postscan_tile<C, P, true>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
+  return postscan_tile<C, P, false>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
 }
 
 // Persistent postscan over tiles first, first + stride, ... below last, for
@@ -664,26 +599,6 @@ __global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P>::MIN_BLOCKS)) po
                                         0u,         prefetch_dist != 0 ? blockIdx.x + prefetch_dist : ~0u,
                                         bp,         0u};
   postscan_job<C, P>(job, hdr, smem);
-}
-
-// One-pass postscan: block i takes the next tile ticket (tiles start in
-// ticket order, which the look-back's waits rely on) and resolves its bucket
-// offsets by decoupled look-back; `starts` holds the global bucket starts
-// from the histogram pass, `lb_status` B zeroed words per tile.
-template <class C, class P>
-__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P>::MIN_BLOCKS)) onepass_postscan_kernel(
-    const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
-    uint32_t* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ starts,
-    uint32_t* lb_status, typename P::Params bp, ScratchHeader* hdr, uint32_t prefetch_dist) {
-  extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ uint32_t s_tile;
-  if (threadIdx.x == 0) s_tile = atomicAdd(&hdr->ticket, 1u);
-  __syncthreads();
-  const uint32_t t = s_tile;
-  const TileJob<typename P::Params> job{kin,     vin, kout, vout, n, num_tiles, t, nullptr, 0u,
-                                        prefetch_dist != 0 ? t + prefetch_dist : ~0u,
-                                        bp,      0u,  lb_status, starts};
-  postscan_job<C, P, true, true>(job, hdr, smem);
 }
 
 // Persistent plain postscan (identifiers with a shared area): block b runs
