@@ -795,7 +795,11 @@ def run_ours(a):
     ms_per_step = total_ms / a.steps
     value = world * n / (ms_per_step * 1e-3) / 1e9
 
-    # End to end through the one-call public API, host buffers, copies inside the step.
+    # End to end through the one-call public API, host buffers, copies inside the
+    # step: every step copies its keys (and values) in from pinned host memory,
+    # runs the multisplit and copies both outputs back.  Steps alternate between
+    # two streams with their own buffers, so one step's copies overlap the
+    # neighbouring steps' work, as a caller streaming batches would run it.
     e2e = None
     if not a.no_e2e:
         hk = torch.empty(n, dtype=torch.int32, pin_memory=True)
@@ -803,33 +807,54 @@ def run_ours(a):
         hv = torch.empty(n, dtype=torch.int32, pin_memory=True) if vals is not None else None
         if hv is not None:
             hv.copy_(vals)
-        hko = torch.empty(n, dtype=torch.int32, pin_memory=True)
-        hvo = torch.empty(n, dtype=torch.int32, pin_memory=True) if vals is not None else None
-        dk, dv = torch.empty_like(keys), (torch.empty_like(vals) if vals is not None else None)
+        lanes = []
+        for _ in range(2):
+            lane_ctx = gms.multisplit_context(B)
+            (gms.multisplit_allocate_key_only if a.keys_only else gms.multisplit_allocate_key_value)(n, lane_ctx)
+            lanes.append({
+                "stream": torch.cuda.Stream(device=dev), "ctx": lane_ctx,
+                "dk": torch.empty_like(keys), "dv": torch.empty_like(vals) if vals is not None else None,
+                "dko": torch.empty_like(keys), "dvo": torch.empty_like(vals) if vals is not None else None,
+                "hko": torch.empty(n, dtype=torch.int32, pin_memory=True),
+                "hvo": torch.empty(n, dtype=torch.int32, pin_memory=True) if vals is not None else None,
+            })
 
-        def e2e_step():
-            dk.copy_(hk, non_blocking=True)
-            if dv is not None:
-                dv.copy_(hv, non_blocking=True)
-            if dv is None:
-                gms.multisplit_key_only(dk, kout, n, ctx, ident)
-            else:
-                gms.multisplit_key_value(dk, dv, kout, vout, n, ctx, ident)
-            hko.copy_(kout, non_blocking=True)
-            if hvo is not None:
-                hvo.copy_(vout, non_blocking=True)
+        def e2e_step(i):
+            ln = lanes[i % 2]
+            with torch.cuda.stream(ln["stream"]):
+                ln["dk"].copy_(hk, non_blocking=True)
+                if hv is not None:
+                    ln["dv"].copy_(hv, non_blocking=True)
+                if hv is None:
+                    gms.multisplit_key_only(ln["dk"], ln["dko"], n, ln["ctx"], ident, stream=ln["stream"])
+                else:
+                    gms.multisplit_key_value(ln["dk"], ln["dv"], ln["dko"], ln["dvo"], n, ln["ctx"], ident,
+                                             stream=ln["stream"])
+                ln["hko"].copy_(ln["dko"], non_blocking=True)
+                if hv is not None:
+                    ln["hvo"].copy_(ln["dvo"], non_blocking=True)
 
-        for _ in range(max(3, a.warmup)):
-            e2e_step()
+        def run_steps(count):
+            start = torch.cuda.Event(enable_timing=True)
+            stop = torch.cuda.Event(enable_timing=True)
+            start.record()
+            for ln in lanes:
+                ln["stream"].wait_event(start)
+            for i in range(count):
+                e2e_step(i)
+            for ln in lanes:
+                ev = torch.cuda.Event()
+                ev.record(ln["stream"])
+                torch.cuda.current_stream().wait_event(ev)
+            stop.record()
+            return start, stop
+
+        run_steps(max(3, a.warmup))
         torch.cuda.synchronize()
-        e_steps = max(3, a.steps // 2)
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e_steps = max(4, a.steps // 2)
         barrier()
         torch.cuda.synchronize()
-        s0.record()
-        for _ in range(e_steps):
-            e2e_step()
-        s1.record()
+        s0, s1 = run_steps(e_steps)
         torch.cuda.synchronize()
         barrier()
         e_ms = s0.elapsed_time(s1) / e_steps
@@ -841,9 +866,16 @@ def run_ours(a):
             e_ms = float(t.item())
         nb = n * 4 * (1 if vals is None else 2)
         e2e = {"value": world * n / (e_ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": e_ms,
-               "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb}
-        # the e2e output must be the same multisplit
-        assert torch.equal(hko, kout.cpu())
+               "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
+               "pipeline": "one-call API from pinned host buffers; steps alternate over 2 streams, so a step's "
+                           "copies overlap its neighbours' work"}
+        # every lane's last output is the same multisplit as the device-resident step
+        ref_k = kout.cpu()
+        for ln in lanes:
+            assert torch.equal(ln["hko"], ref_k)
+            if hv is not None:
+                assert torch.equal(ln["hvo"], vout.cpu())
+        del lanes
 
     per_key_step, per_key_post = algorithmic_bytes(a)
     peak, peak_src = hbm_peak()
