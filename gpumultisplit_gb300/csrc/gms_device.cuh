@@ -200,12 +200,14 @@ struct Identifier {
         for (uint32_t i = 0; i < B; ++i) c += s_split[i] <= key ? 1u : 0u;
         return (c - 1u) & (B - 1);
       } else {
-        // The table bounds c to [lo(t), lo(t+1)].  The cell's first splitter
-        // is tested without a branch; only cells with two or more splitters
-        // need a search over the rest.
+        // The table bounds c to [lo(t), lo(t+1)].  Only keys whose cell holds
+        // a splitter load it (a predicated load: lanes in empty cells add no
+        // shared-memory traffic); only cells with two or more splitters need a
+        // search over the rest.
         const uint32_t e = s_split[B + (key >> (32 - RANGE_LUT_BITS))];
         uint32_t c = e & 0xFFFFu, hi = e >> 16;
-        const uint32_t s0 = s_split[c < B ? c : B - 1];
+        uint32_t s0 = 0;
+        if (c < hi) s0 = s_split[c];
         const bool past_first = c < hi && s0 <= key;
         c += past_first ? 1u : 0u;
         if (past_first && c < hi) {
