@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(C::THREADS) batch_prescan_kernel(const SegDesc
     if (cnt == C::TILE && (reinterpret_cast<uintptr_t>(sd.kin) & 15u) == 0) {
       uint4 v[C::IPT / 4];
       load_tile_v4<C::THREADS, C::IPT>(sd.kin, base, v);
-      count_v4<C::IPT>(v, counter);
+      count_v4<C::THREADS, C::IPT>(v, counter);
     } else {
 #pragma unroll 4
       for (int k = 0; k < C::IPT; ++k) {

@@ -120,6 +120,9 @@ gms_status multisplit_impl(const uint32_t* kin, const uint32_t* vin, uint32_t* k
   c.bp = to_params(desc);
   c.scratch = static_cast<unsigned char*>(scratch);
   c.stream = stream;
+  // Costly identifiers are evaluated once when the scratch has room for a
+  // bucket byte per key (the prescan stores them, the postscan reads them).
+  if (kind_keeps_bucket_bytes(desc->kind) && scratch_bytes >= g.bytes_full) c.bucket_bytes = c.scratch + g.off_buckets;
   return cuda_status(dispatch(desc->kind, c, stages));
 }
 
@@ -339,7 +342,7 @@ gms_status gms_multisplit_scratch_bytes(uint32_t max_elements, uint32_t num_buck
   int logb = 0;
   if (bytes == nullptr) return GMS_ERROR_INVALID_VALUE;
   if (!valid_buckets(num_buckets, &logb)) return GMS_ERROR_UNSUPPORTED_BUCKETS;
-  *bytes = make_geometry(max_elements, logb, key_value != 0).bytes;
+  *bytes = make_geometry(max_elements, logb, key_value != 0).bytes_full;
   return GMS_SUCCESS;
 }
 

@@ -49,11 +49,15 @@ inline uint32_t persistent_grid(Kernel k, int threads, uint32_t work, std::atomi
 
 // Stages of one multisplit with identifier policy P (descriptor kinds here;
 // user functors from the drop-in C++ headers).  `scratch` is laid out as
-// make_geometry(n, LOGB, KV).
+// make_geometry(n, LOGB, KV).  bucket_bytes (n bytes, or null): for
+// identifiers that are costly to evaluate, the prescan stores every key's
+// bucket there and the postscan reads it instead of evaluating the identifier
+// a second time; the prescan and postscan of one multisplit must agree on it.
 template <class P, int LOGB, bool KV>
 cudaError_t launch_multisplit(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n,
                               const typename P::Params& params, unsigned char* scratch, int stages,
-                              cudaStream_t stream) {
+                              cudaStream_t stream, uint8_t* bucket_bytes = nullptr) {
+  if constexpr (P::CHEAP) bucket_bytes = nullptr;
   using S = TileShape<LOGB, KV>;
   using C = TileCfg<LOGB, S::WARPS, S::IPT, KV>;
   const Geometry g = make_geometry(n, LOGB, KV);
@@ -66,13 +70,30 @@ cudaError_t launch_multisplit(const uint32_t* kin, const uint32_t* vin, uint32_t
     static std::atomic<int> per_sm{0};
     auto kern = prescan_kernel<C, P>;
     const uint32_t grid = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm);
-    kern<<<grid, C::THREADS, 0, stream>>>(kin, n, g.num_tiles, matrix, params, hdr, status, g.num_chunks);
+    kern<<<grid, C::THREADS, 0, stream>>>(kin, n, g.num_tiles, matrix, params, hdr, status, g.num_chunks,
+                                          bucket_bytes);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
   if (stages & STAGE_SCAN) {
     cudaError_t e = run_scan(matrix, g.m, status, hdr, stream);
     if (e != cudaSuccess) return e;
+  }
+  if constexpr (!P::CHEAP) {
+    if ((stages & STAGE_POSTSCAN) && bucket_bytes != nullptr) {
+      // Buckets from the prescan: no identifier in the postscan at all.
+      static std::atomic<uint64_t> smem_done{0};
+      static std::atomic<int> per_sm{0};
+      auto kern = postscan_kernel<C, P, true>;
+      constexpr size_t smem = PostLayout<C, P, true>::BYTES;
+      cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
+      if (e != cudaSuccess) return e;
+      const uint32_t wave = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
+      const uint32_t dist = (GMS_PREFETCH_WAVES * wave) / 4u;
+      kern<<<g.num_tiles, C::THREADS, smem, stream>>>(kin, vin, kout, vout, n, g.num_tiles, matrix, params, hdr,
+                                                        dist, bucket_bytes);
+      return cudaGetLastError();
+    }
   }
   if ((stages & STAGE_POSTSCAN) && P::USES_SMEM) {
     // Identifiers with a shared area: persistent blocks prepare it once.
@@ -97,7 +118,7 @@ cudaError_t launch_multisplit(const uint32_t* kin, const uint32_t* vin, uint32_t
     const uint32_t wave = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
     const uint32_t dist = (GMS_PREFETCH_WAVES * wave) / 4u;
     kern<<<g.num_tiles, C::THREADS, smem, stream>>>(kin, vin, kout, vout, n, g.num_tiles, matrix, params, hdr,
-                                                      dist);
+                                                      dist, nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -107,7 +128,7 @@ cudaError_t launch_multisplit(const uint32_t* kin, const uint32_t* vin, uint32_t
 template <int KIND, int LOGB, bool KV>
 cudaError_t run_multisplit_t(const MsCall& c, int stages) {
   return launch_multisplit<DescPolicy<KIND, LOGB>, LOGB, KV>(c.kin, c.vin, c.kout, c.vout, c.n, c.bp, c.scratch,
-                                                             stages, c.stream);
+                                                             stages, c.stream, c.bucket_bytes);
 }
 
 template <int KIND, bool KV>

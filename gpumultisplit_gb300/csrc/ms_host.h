@@ -63,7 +63,9 @@ struct Geometry {
   uint32_t num_chunks = 0;  // scan chunks
   size_t off_status = 0;
   size_t off_matrix = 0;
-  size_t bytes = 0;
+  size_t bytes = 0;         // what every identifier needs
+  size_t off_buckets = 0;   // one byte per key, used by costly identifiers when the scratch has room
+  size_t bytes_full = 0;    // bytes plus the bucket bytes (what gms_multisplit_scratch_bytes reports)
 };
 
 inline Geometry make_geometry(uint32_t n, int logb, bool kv) {
@@ -75,7 +77,15 @@ inline Geometry make_geometry(uint32_t n, int logb, bool kv) {
   g.off_matrix = sizeof(ScratchHeader);
   g.off_status = align_up(g.off_matrix + size_t(g.m) * 4, 256);
   g.bytes = align_up(g.off_status + size_t(g.num_chunks) * 8, 256);
+  g.off_buckets = g.bytes;
+  g.bytes_full = align_up(g.off_buckets + size_t(n), 256);
   return g;
+}
+
+// Identifier kinds costly enough to evaluate once (in the prescan) and keep
+// as one byte per key for the postscan.
+inline bool kind_keeps_bucket_bytes(int kind) {
+  return kind == KIND_RANGE || kind == KIND_DIV || kind == KIND_EVEN_FLOAT;
 }
 
 enum Stage : int { STAGE_PRESCAN = 1, STAGE_SCAN = 2, STAGE_POSTSCAN = 4, STAGE_ALL = 7 };
@@ -91,6 +101,7 @@ struct MsCall {
   BucketParams bp{};
   unsigned char* scratch = nullptr;  // laid out as make_geometry(n, logb, kv)
   cudaStream_t stream = nullptr;
+  uint8_t* bucket_bytes = nullptr;   // in scratch, or null (see launch_multisplit)
 };
 
 // Runs the requested stages (a mask of Stage) of one multisplit.  Defined per

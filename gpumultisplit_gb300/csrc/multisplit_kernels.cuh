@@ -89,7 +89,11 @@ struct KeyCounter {
   // Called by all 32 lanes of the warp together; A selects an accumulator.
   template <int A = 0>
   __device__ __forceinline__ void add(uint32_t key, bool valid) {
-    const uint32_t b = ident(key);
+    add_bucket<A>(ident(key), valid);
+  }
+
+  template <int A = 0>
+  __device__ __forceinline__ void add_bucket(uint32_t b, bool valid) {
     if constexpr (kBallot) {
       uint32_t m = __ballot_sync(~0u, valid);
 #pragma unroll
@@ -152,23 +156,31 @@ __device__ __forceinline__ void load_tile_v4(const uint32_t* __restrict__ keys, 
   for (int k = 0; k < IPT / 4; ++k) v[k] = ld_nc_v4(keys + base + (uint32_t(k) * THREADS + threadIdx.x) * 4u);
 }
 
-template <int IPT, class Counter>
-__device__ __forceinline__ void count_v4(const uint4 (&v)[IPT / 4], Counter& c) {
+// Counts one tile held as 16-byte vectors (thread t holds keys
+// (k*THREADS + t)*4 .. +3 of vector k).  WRITE_BYTES: also stores every key's
+// bucket as one byte at bytes_out[(k*THREADS + t)*4 ..] (four per store).
+template <int THREADS, int IPT, bool WRITE_BYTES = false, class Counter>
+__device__ __forceinline__ void count_v4(const uint4 (&v)[IPT / 4], Counter& c, uint8_t* bytes_out = nullptr) {
 #pragma unroll
   for (int k = 0; k < IPT / 4; ++k) {
-    c.template add<0>(v[k].x, true);
-    c.template add<1>(v[k].y, true);
-    c.template add<2>(v[k].z, true);
-    c.template add<3>(v[k].w, true);
+    const uint32_t b0 = c.ident(v[k].x), b1 = c.ident(v[k].y), b2 = c.ident(v[k].z), b3 = c.ident(v[k].w);
+    c.template add_bucket<0>(b0, true);
+    c.template add_bucket<1>(b1, true);
+    c.template add_bucket<2>(b2, true);
+    c.template add_bucket<3>(b3, true);
+    if constexpr (WRITE_BYTES)
+      reinterpret_cast<uint32_t*>(bytes_out)[uint32_t(k) * THREADS + threadIdx.x] =
+          b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
   }
 }
 
 // Counts tiles first, first+stride, ... (tiles of THREADS*IPT keys) and calls
 // done(tile) after each one.  The next tile's keys are loaded into registers
-// while the current tile is counted, so loads stay in flight.
-template <int THREADS, int IPT, class Counter, class Done>
+// while the current tile is counted, so loads stay in flight.  WRITE_BYTES:
+// every key's bucket is also stored as one byte at bytes_out[key index].
+template <int THREADS, int IPT, bool WRITE_BYTES = false, class Counter, class Done>
 __device__ __forceinline__ void count_tiles(const uint32_t* __restrict__ keys, uint32_t n, uint32_t first,
-                                            uint32_t stride, Counter& c, Done done) {
+                                            uint32_t stride, Counter& c, Done done, uint8_t* bytes_out = nullptr) {
   constexpr uint32_t TILE = uint32_t(THREADS) * IPT;
   const uint32_t num_tiles = uint32_t((uint64_t(n) + TILE - 1) / TILE);
   const bool vec_ok = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0;
@@ -180,7 +192,7 @@ __device__ __forceinline__ void count_tiles(const uint32_t* __restrict__ keys, u
     uint4 nxt[IPT / 4];
     if (next < full_tiles) load_tile_v4<THREADS, IPT>(keys, next * TILE, nxt);
     if (tile < full_tiles) {
-      count_v4<IPT>(cur, c);
+      count_v4<THREADS, IPT, WRITE_BYTES>(cur, c, WRITE_BYTES ? bytes_out + size_t(tile) * TILE : nullptr);
     } else {
       const uint32_t base = tile * TILE;
       const uint32_t cnt = min(TILE, n - base);
@@ -188,7 +200,11 @@ __device__ __forceinline__ void count_tiles(const uint32_t* __restrict__ keys, u
       for (int k = 0; k < IPT; ++k) {
         const uint32_t i = uint32_t(k) * THREADS + threadIdx.x;
         const bool valid = i < cnt;
-        c.add(valid ? keys[base + i] : 0u, valid);
+        const uint32_t b = c.ident(valid ? keys[base + i] : 0u);
+        c.add_bucket(b, valid);
+        if constexpr (WRITE_BYTES) {
+          if (valid) bytes_out[base + i] = uint8_t(b);
+        }
       }
     }
     done(tile);
@@ -201,11 +217,16 @@ __device__ __forceinline__ void count_tiles(const uint32_t* __restrict__ keys, u
 // Persistent grid over the tiles.  Writes counts[b * num_tiles + tile] for
 // every tile and resets the scan state (ticket, chunk status words, error
 // word) for the scan that follows.
+//
+// bucket_bytes (identifiers costly to evaluate; may be null): every key's
+// bucket is also stored there as one byte, so the postscan need not evaluate
+// the identifier again.
 template <class C, class P>
 __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __restrict__ keys, uint32_t n,
                                                              uint32_t num_tiles, uint32_t* __restrict__ counts,
                                                              typename P::Params bp, ScratchHeader* hdr,
-                                                             uint64_t* __restrict__ status, uint32_t num_chunks) {
+                                                             uint64_t* __restrict__ status, uint32_t num_chunks,
+                                                             uint8_t* __restrict__ bucket_bytes) {
   using Counter = KeyCounter<C::LOGB, typename P::Id>;
   __shared__ uint32_t s_hist[Counter::smem_words(C::WARPS)];
   __shared__ uint32_t s_split[P::SMEM_WORDS];  // identifier state (RANGE splitters + table)
@@ -224,10 +245,17 @@ __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __r
   Counter counter(P::make(bp, s_split), s_hist);
   counter.clear_shared();
   __syncthreads();
-  count_tiles<C::THREADS, C::IPT>(keys, n, blockIdx.x, gridDim.x, counter, [&](uint32_t tile) {
+  auto done = [&](uint32_t tile) {
     const uint32_t total = counter.block_total();
     if (tid < C::B) counts[tid * num_tiles + tile] = total;
-  });
+  };
+  if constexpr (!P::CHEAP) {
+    if (bucket_bytes != nullptr) {
+      count_tiles<C::THREADS, C::IPT, true>(keys, n, blockIdx.x, gridDim.x, counter, done, bucket_bytes);
+      return;
+    }
+  }
+  count_tiles<C::THREADS, C::IPT>(keys, n, blockIdx.x, gridDim.x, counter, done);
 }
 
 // Shared-memory layout of the postscan for identifier policy P (bytes), and
@@ -243,9 +271,10 @@ __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __r
 // 32 * IPT keys and a tile holds at most 2^16), except in the bitmap peer mode.
 enum ReorderMode { R_KEYS = 0, R_INDEX16 = 1, R_KEYS_B = 2, R_INDEX16_B = 3 };
 
-template <class C, class P>
+template <class C, class P, bool GIVEN = false>
 struct PostLayout {
   static constexpr bool CHEAP = P::CHEAP;
+  static_assert(!GIVEN || !P::CHEAP, "given bucket bytes are only used for costly identifiers");
   static constexpr int MODE = C::KV ? (CHEAP ? R_INDEX16 : R_INDEX16_B) : (CHEAP ? R_KEYS : R_KEYS_B);
   static constexpr bool INDEXED = MODE == R_INDEX16 || MODE == R_INDEX16_B;
   static constexpr bool BUCKET_BYTES = MODE == R_KEYS_B || MODE == R_INDEX16_B;
@@ -258,7 +287,9 @@ struct PostLayout {
   static constexpr size_t OFF_WH = (OFF_RB + (BUCKET_BYTES ? C::TILE : 0) + 15) & ~size_t(15);
   static constexpr size_t OFF_DELTA = (OFF_WH + size_t(C::WARPS) * C::WB * C::WS * sizeof(WhT) + 15) & ~size_t(15);
   static constexpr size_t OFF_SPLIT = OFF_DELTA + C::B * 4;
-  static constexpr size_t OFF_SCAN = OFF_SPLIT + P::SMEM_WORDS * 4;
+  // With bucket bytes from the prescan the identifier is never evaluated, so
+  // it needs no shared area.
+  static constexpr size_t OFF_SCAN = OFF_SPLIT + (GIVEN ? 0 : P::SMEM_WORDS * 4);
   static constexpr size_t OFF_FLAG = OFF_SCAN + 32 * 4;  // warp totals of the tile scan
   static constexpr size_t OFF_BAR = (OFF_FLAG + 4 + 15) & ~size_t(15);
   static constexpr size_t BYTES = OFF_BAR + 16;
@@ -283,11 +314,15 @@ __device__ __forceinline__ uint32_t peers_by_ballot(uint32_t b) {
 
 // Phases 1-4 of the postscan for one staged tile.  FULL: the tile holds
 // exactly TILE keys, so no per-key validity test is needed.
-template <class C, class P, bool FULL>
+//
+// GIVEN: the tile's buckets were staged as bytes at the bucket-byte area (in
+// input order) by the caller, so the identifier is not evaluated; phase 3
+// overwrites that area with the buckets in sorted order.
+template <class C, class P, bool FULL, bool GIVEN = false>
 __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
                                               uint32_t cnt, uint32_t goff, const typename P::Params& bp,
                                               ScratchHeader* hdr, unsigned char* smem) {
-  using L = PostLayout<C, P>;
+  using L = PostLayout<C, P, GIVEN>;
   using WhT = typename L::WhT;
   constexpr uint32_t B = C::B;
   constexpr int LOGB = C::LOGB;
@@ -323,7 +358,7 @@ __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint3
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
       const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
-      const uint32_t b = ident(s_k[pos]);
+      const uint32_t b = GIVEN ? (uint32_t(s_rb[pos]) & (B - 1)) : ident(s_k[pos]);
       uint32_t m = FULL ? ~0u : __ballot_sync(~0u, pos < cnt);
 #pragma unroll
       for (int i = 0; i < LOGB; ++i) m &= __ballot_sync(~0u, (b >> i) & 1u) ^ xm[i];
@@ -340,7 +375,7 @@ __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint3
       for (int j = 0; j < IPT; ++j) {
         const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
         const bool valid = FULL || pos < cnt;
-        const uint32_t b = ident(s_k[pos]);
+        const uint32_t b = GIVEN ? (uint32_t(s_rb[pos]) & (B - 1)) : ident(s_k[pos]);
         uint32_t* e = reinterpret_cast<uint32_t*>(&wh[b * WS]);
         if (valid) atomicOr(e, 1u << lane);
         __syncwarp();
@@ -356,7 +391,7 @@ __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint3
       for (int j = 0; j < IPT; ++j) {
         const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
         const bool valid = FULL || pos < cnt;
-        const uint32_t b = ident(s_k[pos]);
+        const uint32_t b = GIVEN ? (uint32_t(s_rb[pos]) & (B - 1)) : ident(s_k[pos]);
 #if GMS_PEERS_MODE == 1
         uint32_t peers = __match_any_sync(~0u, b);
 #else
@@ -477,6 +512,7 @@ struct TileJob {
   uint32_t prefetch_tile;    // a later tile of the same arrays to pull into L2 (>= num_tiles: none)
   Params bp;
   uint32_t owner;            // which multisplit of a batch (tiles with one owner share bp)
+  const uint8_t* bucket_bytes;  // every key's bucket, from the prescan (GIVEN postscans only)
 };
 
 // Postscan of one tile, run by a whole block:
@@ -496,10 +532,14 @@ struct TileJob {
 // bulk copy timed out or an offset was out of range; the error is recorded).
 // With `*bar_live` the caller learns whether the tile's mbarrier was
 // initialised (it must be invalidated before the next tile initialises it).
-template <class C, class P, bool PREPARE = true>
+//
+// GIVEN: the prescan stored every key's bucket as a byte (job.bucket_bytes);
+// the tile's bytes are staged with its keys and the identifier is never
+// evaluated (nor prepared).
+template <class C, class P, bool PREPARE = true, bool GIVEN = false>
 __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params>& job, ScratchHeader* hdr,
                                              unsigned char* smem, bool* bar_live = nullptr) {
-  using L = PostLayout<C, P>;
+  using L = PostLayout<C, P, GIVEN>;
   constexpr uint32_t B = C::B;
   constexpr int LOGB = C::LOGB;
   constexpr uint32_t WB = C::WB;
@@ -520,12 +560,18 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params>& 
   if constexpr (C::KV) addr_bits |= reinterpret_cast<uintptr_t>(vin);
   const uint32_t bulk = ((addr_bits & 15u) == 0) ? (cnt & ~3u) : 0u;  // elements moved by the bulk copy
   if (tid == 0) *reinterpret_cast<uint32_t*>(smem + L::OFF_FLAG) = 0u;
+  // Given bucket bytes: whole 16-byte pieces by the bulk copy, the rest below.
+  const uint32_t bulk_b = (GIVEN && bulk != 0) ? (cnt & ~15u) : 0u;
+  uint8_t* s_rb = reinterpret_cast<uint8_t*>(smem + L::OFF_RB);
   if (tid == 0 && bulk != 0) {
     mbar_init(s_bar, 1);
     fence_mbar_init();
-    mbar_arrive_expect_tx(s_bar, (C::KV ? 2u : 1u) * bulk * 4u);
+    mbar_arrive_expect_tx(s_bar, (C::KV ? 2u : 1u) * bulk * 4u + bulk_b);
     bulk_copy_g2s(s_k, kin + base, bulk * 4u, s_bar);
     if constexpr (C::KV) bulk_copy_g2s(s_v, vin + base, bulk * 4u, s_bar);
+    if constexpr (GIVEN) {
+      if (bulk_b != 0) bulk_copy_g2s(s_rb, job.bucket_bytes + base, bulk_b, s_bar);
+    }
     // Pull a tile that starts about one wave of blocks later into L2, so its
     // bulk copy does not wait on DRAM (only full tiles: never past the arrays).
     if (job.prefetch_tile < job.num_tiles - 1u) {
@@ -537,9 +583,12 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params>& 
     s_k[i] = kin[base + i];
     if constexpr (C::KV) s_v[i] = vin[base + i];
   }
+  if constexpr (GIVEN) {
+    for (uint32_t i = bulk_b + tid; i < cnt; i += C::THREADS) s_rb[i] = job.bucket_bytes[base + i];
+  }
   if (bar_live) *bar_live = bulk != 0;
   const uint32_t goff = (tid < B) ? job.offsets[tid * job.num_tiles + job.tile] - job.bias : 0u;
-  if constexpr (PREPARE) P::prepare(s_split, job.bp);
+  if constexpr (PREPARE && !GIVEN) P::prepare(s_split, job.bp);
   if constexpr (LOGB > 5) {
     // the count table as 32-bit words (its byte size is a multiple of 4)
     constexpr uint32_t WORDS = C::WARPS * WB * C::WS * sizeof(typename L::WhT) / 4;
@@ -558,8 +607,8 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params>& 
   }
 
   if (cnt == C::TILE)
-    return postscan_tile<C, P, true>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
-  return postscan_tile<C, P, false>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
+    return postscan_tile<C, P, true, GIVEN>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
+  return postscan_tile<C, P, false, GIVEN>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
 }
 
 // Persistent postscan over tiles first, first + stride, ... below last, for
@@ -587,18 +636,19 @@ __device__ __forceinline__ void postscan_run(uint32_t first, uint32_t last, uint
   }
 }
 
-// Plain postscan: one block per tile of one multisplit.
-template <class C, class P>
-__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P>::MIN_BLOCKS)) postscan_kernel(
+// Plain postscan: one block per tile of one multisplit.  GIVEN: the buckets
+// come from bucket_bytes (written by the prescan).
+template <class C, class P, bool GIVEN = false>
+__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P, GIVEN>::MIN_BLOCKS)) postscan_kernel(
     const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
     uint32_t* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
-    typename P::Params bp, ScratchHeader* hdr, uint32_t prefetch_dist) {
+    typename P::Params bp, ScratchHeader* hdr, uint32_t prefetch_dist, const uint8_t* __restrict__ bucket_bytes) {
   extern __shared__ __align__(128) unsigned char smem[];
   const TileJob<typename P::Params> job{kin,        vin,     kout, vout,
                                         n,          num_tiles, blockIdx.x, offsets,
                                         0u,         prefetch_dist != 0 ? blockIdx.x + prefetch_dist : ~0u,
-                                        bp,         0u};
-  postscan_job<C, P>(job, hdr, smem);
+                                        bp,         0u,      bucket_bytes};
+  postscan_job<C, P, true, GIVEN>(job, hdr, smem);
 }
 
 // Persistent plain postscan (identifiers with a shared area): block b runs

@@ -26,10 +26,12 @@ inline bool generic_log2(uint32_t b, int* logb) {
 
 template <class F, bool KV>
 cudaError_t generic_launch(int logb, const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout,
-                           uint32_t n, const F& f, unsigned char* scratch, cudaStream_t s) {
+                           uint32_t n, const F& f, unsigned char* scratch, cudaStream_t s, uint8_t* bucket_bytes) {
   switch (logb) {
-#define GMS_GENERIC_CASE(L) \
-  case L: return launch_multisplit<FunctorPolicy<F, L>, L, KV>(kin, vin, kout, vout, n, f, scratch, STAGE_ALL, s);
+#define GMS_GENERIC_CASE(L)                                                                                    \
+  case L:                                                                                                      \
+    return launch_multisplit<FunctorPolicy<F, L>, L, KV>(kin, vin, kout, vout, n, f, scratch, STAGE_ALL, s, \
+                                                         bucket_bytes);
     GMS_GENERIC_CASE(1)
     GMS_GENERIC_CASE(2)
     GMS_GENERIC_CASE(3)
@@ -63,8 +65,11 @@ gms_status generic_multisplit(const uint32_t* kin, const uint32_t* vin, uint32_t
   const Geometry g = make_geometry(n, logb, kv);
   if (scratch_bytes < g.bytes) return GMS_ERROR_SCRATCH_TOO_SMALL;
   auto* sc = static_cast<unsigned char*>(scratch);
-  cudaError_t e = kv ? generic_launch<F, true>(logb, kin, vin, kout, vout, n, f, sc, s)
-                     : generic_launch<F, false>(logb, kin, nullptr, kout, nullptr, n, f, sc, s);
+  // A user functor's cost is unknown: with room for a byte per key, its
+  // buckets are computed once (prescan) and read back (postscan).
+  uint8_t* bb = scratch_bytes >= g.bytes_full ? sc + g.off_buckets : nullptr;
+  cudaError_t e = kv ? generic_launch<F, true>(logb, kin, vin, kout, vout, n, f, sc, s, bb)
+                     : generic_launch<F, false>(logb, kin, nullptr, kout, nullptr, n, f, sc, s, bb);
   if (e == cudaSuccess && h_offsets) {
     e = cudaMemcpy2DAsync(h_offsets, sizeof(uint32_t), sc + g.off_matrix, size_t(g.num_tiles) * 4, sizeof(uint32_t),
                           num_buckets, cudaMemcpyDeviceToHost, s);

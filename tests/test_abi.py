@@ -46,6 +46,12 @@ def gms_lib_():
     return gms.load()
 
 
+def multisplit_min_bytes(n, B, kv):
+    """Scratch a multisplit needs without the optional byte per key (what the
+    sorts reserve for their passes: bit-field digits are cheap to evaluate)."""
+    return scratch_bytes(n, B, kv)[1] - (n + 255) // 256 * 256
+
+
 @pytest.mark.parametrize("B", [2, 4, 8, 16, 32, 64, 128, 256])
 @pytest.mark.parametrize("kv", [0, 1])
 def test_scratch_and_geometry(gms_lib, B, kv):
@@ -57,7 +63,7 @@ def test_scratch_and_geometry(gms_lib, B, kv):
                                                ctypes.byref(off)) == 0
         assert tiles.value == (n + tile.value - 1) // tile.value
         assert off.value == 256  # the count matrix always starts after the 256-byte header
-        assert nbytes >= 256 + 4 * B * tiles.value
+        assert nbytes >= 256 + 4 * B * tiles.value + n  # matrix, plus a bucket byte per key
         assert nbytes % 256 == 0
 
 
@@ -103,8 +109,8 @@ def test_sort_scratch_covers_both_digit_widths(gms_lib):
         for kv in (0, 1):
             sb = ctypes.c_size_t()
             assert gms_lib.gms_sort_7bit_scratch_bytes(n, kv, ctypes.byref(sb)) == 0
-            _, m16 = scratch_bytes(n, 16, kv)
-            _, m128 = scratch_bytes(n, 128, kv)
+            m16 = multisplit_min_bytes(n, 16, kv)
+            m128 = multisplit_min_bytes(n, 128, kv)
             assert sb.value >= max(m16, m128) + 4 * n * (1 + kv)
 
 
@@ -116,7 +122,7 @@ def test_sort_scratch_all_digit_widths(gms_lib):
             for kv in (0, 1):
                 sb = ctypes.c_size_t()
                 assert gms_lib.gms_sort_scratch_bytes(n, bits, kv, ctypes.byref(sb)) == 0
-                need = max(scratch_bytes(n, b, kv)[1] for b in bs) + 4 * n * (1 + kv)
+                need = max(multisplit_min_bytes(n, b, kv) for b in bs) + 4 * n * (1 + kv)
                 assert sb.value >= need, (bits, n, kv)
     sb = ctypes.c_size_t()
     for bad in (3, 9, 0):
@@ -127,7 +133,7 @@ def test_partial_key_sort_scratch_and_checks(gms_lib):
     sb = ctypes.c_size_t()
     for begin, end, digit, widths in ((0, 32, 8, (256,)), (3, 17, 5, (32, 16)), (20, 21, 6, (2,))):
         assert gms_lib.gms_sort_bits_scratch_bytes(1 << 20, begin, end, digit, 1, ctypes.byref(sb)) == 0
-        need = max(scratch_bytes(1 << 20, b, 1)[1] for b in widths) + 8 * (1 << 20)
+        need = max(multisplit_min_bytes(1 << 20, b, 1) for b in widths) + 8 * (1 << 20)
         assert sb.value >= need
     assert gms_lib.gms_sort_bits_scratch_bytes(100, 9, 9, 8, 0, ctypes.byref(sb)) == 0 and sb.value == 0
     for begin, end, digit in ((5, 4, 8), (0, 33, 8), (-1, 8, 8), (0, 8, 3), (0, 8, 9)):

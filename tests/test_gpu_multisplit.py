@@ -219,3 +219,60 @@ def test_range_adversarial_splitters(gms_lib, oracle_mod, B, with_values):
     hist = torch.zeros(B, dtype=torch.int32, device="cuda")
     gms.histogram_range(to_dev(keys), n, hist, B, d_spl)
     np.testing.assert_array_equal(hist.cpu().numpy(), o.histogram(keys, o.Desc(o.RANGE, B, splitters=spl)))
+
+
+@pytest.mark.parametrize("kind", [1, 3, 5], ids=lambda k: KIND_NAMES[k])
+@pytest.mark.parametrize("B", [8, 64, 256])
+@pytest.mark.parametrize("with_values", [False, True], ids=["keys", "pairs"])
+def test_bucket_bytes_and_fallback(gms_lib, oracle_mod, kind, B, with_values):
+    """Costly identifiers (div, range, even-float) are evaluated once when the
+    scratch holds a byte per key, and twice when it holds only the minimum;
+    both give the oracle's output, through the one call and the three stages,
+    full tiles, a ragged tail and misaligned buffers alike."""
+    import ctypes
+
+    o = oracle_mod
+    n = 3 * 4096 + 1234
+    keys = datagen.as_u32(datagen.uniform_u32(n, 4000 + kind * 7 + B))
+    vals = np.arange(n, dtype=np.uint32) if with_values else None
+    ident, d, keep = identifiers(o, kind, B)
+    rk, rv, roffs = o.multisplit(keys, d, vals)
+    full = ctypes.c_size_t()
+    assert gms_lib.gms_multisplit_scratch_bytes(n, B, int(with_values), ctypes.byref(full)) == 0
+    minimum = full.value - (n + 255) // 256 * 256
+    desc = ident.desc(B)
+    stream = torch.cuda.current_stream().cuda_stream
+    for nbytes in (full.value, minimum):
+        for misalign in (0, 1):
+            scratch = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+            dk = to_dev(keys, misalign)
+            dv = to_dev(vals, misalign) if with_values else None
+            ok = to_dev(np.zeros(n, np.uint32), misalign)
+            ov = to_dev(np.zeros(n, np.uint32), misalign) if with_values else None
+            offs = (ctypes.c_uint32 * B)()
+            if with_values:
+                st = gms_lib.gms_multisplit_key_value(dk.data_ptr(), dv.data_ptr(), ok.data_ptr(), ov.data_ptr(), n,
+                                                      ctypes.byref(desc), scratch.data_ptr(), nbytes, offs, stream)
+            else:
+                st = gms_lib.gms_multisplit_key_only(dk.data_ptr(), ok.data_ptr(), n, ctypes.byref(desc),
+                                                     scratch.data_ptr(), nbytes, offs, stream)
+            assert st == 0
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(host(ok), rk)
+            if with_values:
+                np.testing.assert_array_equal(host(ov), rv)
+            assert list(offs) == [int(x) for x in roffs]
+            # the three stages with the same scratch size
+            ok.zero_()
+            args = (ctypes.byref(desc), int(with_values), scratch.data_ptr(), nbytes, stream)
+            assert gms_lib.gms_multisplit_prescan(dk.data_ptr(), n, *args) == 0
+            assert gms_lib.gms_multisplit_scan(n, *args) == 0
+            assert gms_lib.gms_multisplit_postscan(dk.data_ptr(), dv.data_ptr() if with_values else None,
+                                                   ok.data_ptr(), ov.data_ptr() if with_values else None, n,
+                                                   ctypes.byref(desc), scratch.data_ptr(), nbytes, stream) == 0
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(host(ok), rk)
+            code = ctypes.c_uint32()
+            gms_lib.gms_read_device_error(scratch.data_ptr(), ctypes.byref(code), stream)
+            assert code.value == 0
+    del keep
