@@ -91,7 +91,11 @@ gms_status gms_read_device_error(const void* d_scratch, uint32_t* h_code, gms_st
 
 /* ------------------------------------------------------------ multisplit */
 /* Replaces multisplit_allocate_key_only / _key_value (src/api/multisplit.cuh:50-74):
- * scratch bytes for calls with n <= max_elements. */
+ * scratch bytes for calls with n <= max_elements.  The size includes one byte
+ * per key that identifiers costly to evaluate (range, div, even-float) use to
+ * evaluate the identifier once instead of twice; a scratch without that room
+ * (max_elements bytes less, rounded up to 256) still works, more slowly for
+ * those identifiers. */
 gms_status gms_multisplit_scratch_bytes(uint32_t max_elements, uint32_t num_buckets, int key_value,
                                         size_t* bytes);
 
@@ -111,8 +115,10 @@ gms_status gms_multisplit_key_value(const uint32_t* d_key_in, const uint32_t* d_
 /* The three stages of one multisplit, callable one by one (the reference runs
  * them as prescan kernel, cub::DeviceScan::ExclusiveSum, postscan kernel:
  * src/api/multisplit.cuh:212-272).  Scratch sized by gms_multisplit_scratch_bytes
- * for the same n, B and key_value.  After gms_multisplit_scan the count matrix in
- * scratch holds global offsets, bucket-major: offset(b, tile) at b*num_tiles+tile. */
+ * for the same n, B and key_value, and the same scratch_bytes passed to all
+ * three (it decides whether the prescan leaves bucket bytes for the postscan).
+ * After gms_multisplit_scan the count matrix in scratch holds global offsets,
+ * bucket-major: offset(b, tile) at b*num_tiles+tile. */
 gms_status gms_multisplit_prescan(const uint32_t* d_key_in, uint32_t n, const gms_bucket_desc* desc,
                                   int key_value, void* d_scratch, size_t scratch_bytes, gms_stream_t stream);
 gms_status gms_multisplit_scan(uint32_t n, const gms_bucket_desc* desc, int key_value, void* d_scratch,
