@@ -37,7 +37,7 @@ struct gms_batch_s {
   std::vector<gms::SegDesc> segs;
   std::vector<gms::BatchClass> classes;
   std::vector<gms::ScanGroup> groups;
-  size_t off_segs = 0, off_maps = 0, off_matrix = 0, off_status = 0, bytes = 0;
+  size_t off_segs = 0, off_maps = 0, off_matrix = 0, off_status = 0, off_bytes = 0, bytes = 0;
   uint32_t max_chunks = 0;
   // Bound scratch (tables uploaded) and the captured graph for it.
   std::mutex mu;
@@ -88,6 +88,7 @@ cudaError_t launch_all(gms_batch_s* b, unsigned char* scratch, cudaStream_t s) {
   BatchClassLaunch L;
   L.segs = reinterpret_cast<const SegDesc*>(scratch + b->off_segs);
   L.matrix = matrix;
+  L.byte_area = scratch + b->off_bytes;
   L.hdr = hdr;
   L.stream = s;
   for (int stage : {int(STAGE_PRESCAN), int(STAGE_POSTSCAN)}) {
@@ -132,7 +133,7 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
     return GMS_ERROR_INVALID_VALUE;
   auto* b = new gms_batch_s();
   std::map<std::tuple<int, int, bool, int>, size_t> class_index;
-  uint64_t matrix_total = 0, group_n = 0;
+  uint64_t matrix_total = 0, group_n = 0, byte_total = 0;
   ScanGroup group;
   for (uint32_t i = 0; i < count; ++i) {
     const gms_segment& sg = segments[i];
@@ -179,6 +180,11 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
     }
     d.base = uint32_t(group_n);
     d.matrix_off = uint32_t(matrix_total);
+    d.bytes_off = 0;
+    if (kind_keeps_bucket_bytes(kind)) {  // one bucket byte per key, 16-byte aligned per segment
+      d.bytes_off = byte_total;
+      byte_total += (uint64_t(sg.n) + 15) & ~uint64_t(15);
+    }
     group_n += sg.n;
     matrix_total += entries;
     if (matrix_total > 0xFFFFFFFFull) {
@@ -217,7 +223,8 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
   b->off_matrix = off;
   off = align_up(off + size_t(matrix_total) * 4, 256);
   b->off_status = off;
-  b->bytes = align_up(off + size_t(b->max_chunks) * 8, 256);
+  b->off_bytes = align_up(off + size_t(b->max_chunks) * 8, 256);
+  b->bytes = align_up(b->off_bytes + size_t(byte_total), 256);
   *batch = b;
   return GMS_SUCCESS;
 }

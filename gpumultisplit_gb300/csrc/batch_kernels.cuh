@@ -7,7 +7,9 @@
 // All segments' count matrices are laid end to end and scanned as one array,
 // so a scanned offset is the segment's start within its scan group (`base`,
 // the sum of the n of earlier segments in the group) plus the offset inside
-// the segment; the postscan subtracts `base`.
+// the segment; the postscan subtracts `base`.  Segments whose identifier is
+// costly (range, div, even-float) get a byte per key in the batch's byte
+// area: the prescan stores each key's bucket there and the postscan reads it.
 #pragma once
 
 #include "multisplit_kernels.cuh"
@@ -24,6 +26,7 @@ struct SegDesc {
   uint32_t matrix_off;  // first count of this segment in the batch count matrix
   uint32_t base;        // start of this segment in its scan group
   BucketParams bp;
+  uint64_t bytes_off;   // costly identifiers: this segment's bucket bytes in the batch's byte area
 };
 
 // Persistent prescan over the tiles of one class.  Tiles of one segment are
@@ -33,8 +36,10 @@ template <class C, int KIND>
 __global__ void __launch_bounds__(C::THREADS) batch_prescan_kernel(const SegDesc* __restrict__ segs,
                                                                    const uint2* __restrict__ tile_map,
                                                                    uint32_t class_tiles,
-                                                                   uint32_t* __restrict__ matrix) {
+                                                                   uint32_t* __restrict__ matrix,
+                                                                   uint8_t* __restrict__ byte_area) {
   using P = DescPolicy<KIND, C::LOGB>;
+  constexpr bool BYTES = !P::CHEAP;
   using Counter = KeyCounter<C::LOGB, typename P::Id>;
   __shared__ uint32_t s_hist[Counter::smem_words(C::WARPS)];
   __shared__ uint32_t s_split[P::SMEM_WORDS];
@@ -56,16 +61,21 @@ __global__ void __launch_bounds__(C::THREADS) batch_prescan_kernel(const SegDesc
     }
     const uint32_t base = m.y * C::TILE;
     const uint32_t cnt = min(C::TILE, sd.n - base);
+    uint8_t* bytes = BYTES ? byte_area + sd.bytes_off + base : nullptr;
     if (cnt == C::TILE && (reinterpret_cast<uintptr_t>(sd.kin) & 15u) == 0) {
       uint4 v[C::IPT / 4];
       load_tile_v4<C::THREADS, C::IPT>(sd.kin, base, v);
-      count_v4<C::THREADS, C::IPT>(v, counter);
+      count_v4<C::THREADS, C::IPT, BYTES>(v, counter, bytes);
     } else {
 #pragma unroll 4
       for (int k = 0; k < C::IPT; ++k) {
         const uint32_t i = uint32_t(k) * C::THREADS + tid;
         const bool valid = i < cnt;
-        counter.add(valid ? sd.kin[base + i] : 0u, valid);
+        const uint32_t b = counter.ident(valid ? sd.kin[base + i] : 0u);
+        counter.add_bucket(b, valid);
+        if constexpr (BYTES) {
+          if (valid) bytes[i] = uint8_t(b);
+        }
       }
     }
     const uint32_t total = counter.block_total();
@@ -73,41 +83,21 @@ __global__ void __launch_bounds__(C::THREADS) batch_prescan_kernel(const SegDesc
   }
 }
 
-// One block per tile of one class.
+// One block per tile of one class; costly identifiers read the buckets the
+// prescan stored.
 template <class C, int KIND>
-__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, DescPolicy<KIND, C::LOGB>>::MIN_BLOCKS))
+__global__ void __launch_bounds__(C::THREADS,
+                                  (PostLayout<C, DescPolicy<KIND, C::LOGB>, !DescPolicy<KIND, C::LOGB>::CHEAP>::MIN_BLOCKS))
     batch_postscan_kernel(const SegDesc* __restrict__ segs, const uint2* __restrict__ tile_map,
-                          const uint32_t* __restrict__ matrix, ScratchHeader* hdr) {
+                          const uint32_t* __restrict__ matrix, ScratchHeader* hdr, const uint8_t* byte_area) {
+  using P = DescPolicy<KIND, C::LOGB>;
   extern __shared__ __align__(128) unsigned char smem[];
   const uint2 m = tile_map[blockIdx.x];
   const SegDesc& sd = segs[m.x];
   const TileJob<BucketParams> job{sd.kin, sd.vin,  sd.kout, sd.vout, sd.n,  sd.num_tiles,
-                                  m.y,    matrix + sd.matrix_off, sd.base, ~0u, sd.bp, m.x};
-  postscan_job<C, DescPolicy<KIND, C::LOGB>>(job, hdr, smem);
-}
-
-// Persistent form for identifiers with a shared area (RANGE): block b runs a
-// contiguous range of the class's tile map and prepares the identifier again
-// only when the segment changes.  The prefetch pulls the next tile of the same
-// segment into L2.
-template <class C, int KIND>
-__global__ void __launch_bounds__(C::THREADS, (PostLayout<C, DescPolicy<KIND, C::LOGB>>::MIN_BLOCKS))
-    batch_postscan_persistent_kernel(const SegDesc* __restrict__ segs, const uint2* __restrict__ tile_map,
-                                     uint32_t class_tiles, const uint32_t* __restrict__ matrix, ScratchHeader* hdr) {
-  extern __shared__ __align__(128) unsigned char smem[];
-  const uint32_t per = (class_tiles + gridDim.x - 1) / gridDim.x;
-  const uint32_t first = blockIdx.x * per;
-  const uint32_t last = min(first + per, class_tiles);
-  postscan_run<C, DescPolicy<KIND, C::LOGB>>(
-      first, last, 1u,
-      [&](uint32_t t, uint32_t next) {
-        const uint2 m = tile_map[t];
-        const SegDesc& sd = segs[m.x];
-        const uint32_t pf = (next != ~0u && tile_map[next].x == m.x) ? tile_map[next].y : ~0u;
-        return TileJob<BucketParams>{sd.kin, sd.vin, sd.kout, sd.vout, sd.n, sd.num_tiles, m.y,
-                                     matrix + sd.matrix_off, sd.base, pf, sd.bp, m.x};
-      },
-      hdr, smem);
+                                  m.y,    matrix + sd.matrix_off, sd.base, ~0u, sd.bp, m.x,
+                                  P::CHEAP ? nullptr : byte_area + sd.bytes_off};
+  postscan_job<C, P, true, !P::CHEAP>(job, hdr, smem);
 }
 
 }  // namespace gms

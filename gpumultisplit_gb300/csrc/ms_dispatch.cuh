@@ -164,24 +164,16 @@ cudaError_t run_batch_class_t(const BatchClassLaunch& c, int stage) {
       static std::atomic<int> per_sm{0};
       auto kern = batch_prescan_kernel<C, KIND>;
       const uint32_t grid = persistent_grid(kern, C::THREADS, c.class_tiles, per_sm);
-      kern<<<grid, C::THREADS, 0, c.stream>>>(c.segs, c.tile_map, c.class_tiles, c.matrix);
+      kern<<<grid, C::THREADS, 0, c.stream>>>(c.segs, c.tile_map, c.class_tiles, c.matrix, c.byte_area);
       return cudaGetLastError();
     }
     static std::atomic<uint64_t> smem_done{0};
-    constexpr size_t smem = PostLayout<C, DescPolicy<KIND, LOGB>>::BYTES;
-    if constexpr (DescPolicy<KIND, LOGB>::USES_SMEM) {
-      static std::atomic<int> per_sm{0};
-      auto kern = batch_postscan_persistent_kernel<C, KIND>;
-      cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
-      if (e != cudaSuccess) return e;
-      const uint32_t grid = persistent_grid(kern, C::THREADS, c.class_tiles, per_sm, smem);
-      kern<<<grid, C::THREADS, smem, c.stream>>>(c.segs, c.tile_map, c.class_tiles, c.matrix, c.hdr);
-      return cudaGetLastError();
-    }
+    using P = DescPolicy<KIND, LOGB>;
+    constexpr size_t smem = PostLayout<C, P, !P::CHEAP>::BYTES;
     auto kern = batch_postscan_kernel<C, KIND>;
     cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
     if (e != cudaSuccess) return e;
-    kern<<<c.class_tiles, C::THREADS, smem, c.stream>>>(c.segs, c.tile_map, c.matrix, c.hdr);
+    kern<<<c.class_tiles, C::THREADS, smem, c.stream>>>(c.segs, c.tile_map, c.matrix, c.hdr, c.byte_area);
     return cudaGetLastError();
   }
 }

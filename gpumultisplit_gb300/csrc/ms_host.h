@@ -127,6 +127,7 @@ struct BatchClassLaunch {
   const uint2* tile_map = nullptr;  // device, class_tiles entries of (segment, tile)
   uint32_t class_tiles = 0;
   uint32_t* matrix = nullptr;       // device, the batch count matrix
+  uint8_t* byte_area = nullptr;     // device, bucket bytes of segments with costly identifiers
   ScratchHeader* hdr = nullptr;
   cudaStream_t stream = nullptr;
 };
