@@ -222,7 +222,7 @@ def run_batched(dev, reps: int = 3):
 
     # Tile shapes per (B, size class) for this device, then the plan from the tuned table.
     t0 = time.perf_counter()
-    gms.autotune(buckets=(2, 8, 32, 256), key_value=(True,), keys_per_trial=1 << 24, reps=3)
+    gms.autotune(buckets=(2, 8, 32, 256), key_value=(True,), keys_per_trial=1 << 25, reps=5)
     autotune_s = time.perf_counter() - t0
     table = gms.tuning_table()
     chosen = {f"B{B}": [gms.tile_variant_shape(table[(B, True, c)])[2] for c in range(8)] for B in (2, 8, 32, 256)}

@@ -46,6 +46,10 @@ struct gms_batch_s {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   void* graph_scratch = nullptr;
+  // Side streams and events of gms_batch_run: the classes of one stage run on
+  // several streams so small classes overlap large ones (created on first use).
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> events;
 };
 
 namespace gms {
@@ -77,9 +81,66 @@ cudaError_t dispatch_variant(const BatchClassLaunch& c, int stage) {
 }
 static_assert(kNumTileVariants == 4, "dispatch_variant covers every tile variant");
 
+constexpr int kSideStreams = 4;
+
+cudaError_t ensure_side_streams(gms_batch_s* b) {
+  if (!b->side.empty()) return cudaSuccess;
+  for (int i = 0; i < kSideStreams; ++i) {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      if (st) cudaStreamDestroy(st);
+      return e;
+    }
+    b->side.push_back(st);
+    b->events.push_back(ev);
+  }
+  cudaEvent_t fork = nullptr;
+  cudaError_t e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) b->events.push_back(fork);  // last event: the fork point
+  return e;
+}
+
+// Launches one stage of every class.  With side streams the classes (largest
+// first) are dealt round-robin to the side streams, which fork from and join
+// back into `s`, so a stage's kernels of different classes can run at once.
+cudaError_t launch_classes(gms_batch_s* b, BatchClassLaunch L, unsigned char* scratch, cudaStream_t s, int stage,
+                           bool fork) {
+  const size_t nc = b->classes.size();
+  const int lanes = fork && nc > 1 ? int(std::min<size_t>(nc, b->side.size())) : 0;
+  cudaError_t e = cudaSuccess;
+  if (lanes > 0) {
+    e = cudaEventRecord(b->events.back(), s);
+    for (int i = 0; e == cudaSuccess && i < lanes; ++i) e = cudaStreamWaitEvent(b->side[i], b->events.back(), 0);
+    if (e != cudaSuccess) return e;
+  }
+  std::vector<size_t> order(nc);
+  for (size_t i = 0; i < nc; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t x, size_t y) { return b->classes[x].tiles.size() > b->classes[y].tiles.size(); });
+  for (size_t k = 0; k < nc; ++k) {
+    const BatchClass& c = b->classes[order[k]];
+    L.logb = c.logb;
+    L.kv = c.kv;
+    L.variant = c.variant;
+    L.tile_map = reinterpret_cast<const uint2*>(scratch + c.map_off);
+    L.class_tiles = uint32_t(c.tiles.size());
+    L.stream = lanes > 0 ? b->side[k % size_t(lanes)] : s;
+    e = run_batch_class(c.kind, L, stage);
+    if (e != cudaSuccess) return e;
+  }
+  for (int i = 0; e == cudaSuccess && i < lanes; ++i) {
+    e = cudaEventRecord(b->events[i], b->side[i]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, b->events[i], 0);
+  }
+  return e;
+}
+
 // The launch sequence of one run: reset the error word, prescan every class,
 // scan every group (ticket and status words reset first), postscan every class.
-cudaError_t launch_all(gms_batch_s* b, unsigned char* scratch, cudaStream_t s) {
+cudaError_t launch_all(gms_batch_s* b, unsigned char* scratch, cudaStream_t s, bool fork = false) {
   auto* hdr = reinterpret_cast<ScratchHeader*>(scratch);
   auto* matrix = reinterpret_cast<uint32_t*>(scratch + b->off_matrix);
   auto* status = reinterpret_cast<uint64_t*>(scratch + b->off_status);
@@ -101,15 +162,8 @@ cudaError_t launch_all(gms_batch_s* b, unsigned char* scratch, cudaStream_t s) {
         if (e != cudaSuccess) return e;
       }
     }
-    for (const BatchClass& c : b->classes) {
-      L.logb = c.logb;
-      L.kv = c.kv;
-      L.variant = c.variant;
-      L.tile_map = reinterpret_cast<const uint2*>(scratch + c.map_off);
-      L.class_tiles = uint32_t(c.tiles.size());
-      e = run_batch_class(c.kind, L, stage);
-      if (e != cudaSuccess) return e;
-    }
+    e = launch_classes(b, L, scratch, s, stage, fork);
+    if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
@@ -282,7 +336,9 @@ gms_status gms_batch_run(gms_batch_t b, void* d_scratch, size_t scratch_bytes, i
     if (e != cudaSuccess) return to_status(e);
     b->bound = d_scratch;
   }
-  if (!use_graph) return to_status(launch_all(b, scratch, stream));
+  e = ensure_side_streams(b);
+  if (e != cudaSuccess) return to_status(e);
+  if (!use_graph) return to_status(launch_all(b, scratch, stream, true));
 
   if (b->exec == nullptr || b->graph_scratch != d_scratch) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -295,7 +351,7 @@ gms_status gms_batch_run(gms_batch_t b, void* d_scratch, size_t scratch_bytes, i
     }
     e = cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return to_status(e);
-    const cudaError_t le = launch_all(b, scratch, b->capture_stream);
+    const cudaError_t le = launch_all(b, scratch, b->capture_stream, true);
     e = cudaStreamEndCapture(b->capture_stream, &b->graph);
     if (le != cudaSuccess) return to_status(le);
     if (e != cudaSuccess) return to_status(e);
@@ -346,6 +402,8 @@ gms_status gms_batch_destroy(gms_batch_t b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+  for (cudaStream_t st : b->side) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : b->events) cudaEventDestroy(ev);
   delete b;
   return GMS_SUCCESS;
 }

@@ -21,6 +21,13 @@ namespace {
 
 constexpr int kMaxLogB = 8;
 
+// Built-in choice for a size class: the tile that just holds the segment up
+// to 2048 keys, the plain path's 4096-key tile above.
+int builtin_variant(int size_class_index) { return size_class_index == 0 ? 2 : (size_class_index == 1 ? 1 : 0); }
+
+// Relative gain another variant needs over the built-in one to replace it.
+constexpr float kTuneMargin = 0.03f;
+
 struct Table {
   std::mutex mu;
   int v[kMaxLogB][2][kNumSizeClasses];
@@ -28,7 +35,7 @@ struct Table {
   void reset() {
     for (int l = 0; l < kMaxLogB; ++l)
       for (int kv = 0; kv < 2; ++kv)
-        for (int c = 0; c < kNumSizeClasses; ++c) v[l][kv][c] = c == 0 ? 2 : (c == 1 ? 1 : 0);
+        for (int c = 0; c < kNumSizeClasses; ++c) v[l][kv][c] = builtin_variant(c);
   }
 };
 
@@ -216,17 +223,27 @@ gms_status gms_autotune(uint32_t bucket_mask, uint32_t key_value_mask, uint32_t 
           sg.n = seg_n;
           sg.desc = gms_bucket_desc{GMS_BUCKET_DELTA, 1u << logb, 0u, 0u, 0u, 0.0f, nullptr};
         }
-        float best = -1.0f;
+        // The built-in entry keeps its place unless another variant is faster
+        // by more than kTuneMargin (timing noise must not flip the table).
+        const int builtin = builtin_variant(c);
+        float builtin_ms = -1.0f, other_ms = -1.0f;
+        int other = -1;
         for (int v = 0; v < kNumTileVariants; ++v) {
           if (!variant_valid(v, logb)) continue;
           float ms = -1.0f;
           const gms_status st = time_plan(tb, segs, v, reps, stream, &ms);
           if (st != GMS_SUCCESS) return st;
-          if (ms >= 0.0f && (best < 0.0f || ms < best)) {
-            best = ms;
-            best_v[logb - 1][kv][c] = v;
+          if (ms < 0.0f) continue;
+          if (v == builtin) {
+            builtin_ms = ms;
+          } else if (other_ms < 0.0f || ms < other_ms) {
+            other_ms = ms;
+            other = v;
           }
         }
+        const bool take_other = other >= 0 && (builtin_ms < 0.0f || other_ms < builtin_ms * (1.0f - kTuneMargin));
+        best_v[logb - 1][kv][c] = take_other ? other : builtin;
+        const float best = take_other ? other_ms : builtin_ms;
         if (h_ms_out) h_ms_out[((logb - 1) * 2 + kv) * kNumSizeClasses + c] = best;
       }
     }

@@ -267,6 +267,7 @@ gms_status gms_tuning_reset(void);
  * key-value) and every size class, builds a batch of segments of the class's
  * size (delta identifier, about keys_per_trial keys in all), times each valid
  * variant as a graph replay on `stream` (best of `reps`) and stores the fastest
+ * (the built-in entry stays unless another variant is more than 3% faster)
  * in the table.  It allocates its own device buffers (about 16 bytes per
  * trial key) and frees them before returning; it synchronises `stream`.
  * h_ms_out (optional) receives the best time per entry, indexed
