@@ -31,6 +31,13 @@
 #define GMS_PEERS_MODE 0
 #endif
 
+// Threads per SM the key-only postscan's register budget is sized for: six
+// 256-thread blocks (40 registers) measured 3-5% faster than four (64) at
+// B <= 32 and equal above.
+#ifndef GMS_KEYS_RESIDENT_THREADS
+#define GMS_KEYS_RESIDENT_THREADS 1536
+#endif
+
 namespace gms {
 
 // Tile geometry of one (B, key/value) instance.
@@ -294,7 +301,8 @@ struct PostLayout {
   static constexpr size_t OFF_BAR = (OFF_FLAG + 4 + 15) & ~size_t(15);
   static constexpr size_t BYTES = OFF_BAR + 16;
   // Blocks per SM the register budget is sized for (64 registers at 16 keys per thread).
-  static constexpr int MIN_BLOCKS = (C::IPT <= 8 ? 1536 : 1024) / C::THREADS > 0 ? (C::IPT <= 8 ? 1536 : 1024) / C::THREADS : 1;
+  static constexpr int RESIDENT_THREADS = C::IPT <= 8 ? 1536 : (C::KV ? 1024 : GMS_KEYS_RESIDENT_THREADS);
+  static constexpr int MIN_BLOCKS = RESIDENT_THREADS / C::THREADS > 0 ? RESIDENT_THREADS / C::THREADS : 1;
 };
 
 // Peer mask (lanes of this warp whose key in this slot has bucket b) from
