@@ -37,6 +37,11 @@
 #ifndef GMS_KEYS_RESIDENT_THREADS
 #define GMS_KEYS_RESIDENT_THREADS 1536
 #endif
+// The same for the key-value postscan: four blocks of 64 registers (five
+// blocks gained 2% at B = 64 and lost 2% at B = 256; six spilled and lost more).
+#ifndef GMS_PAIRS_RESIDENT_THREADS
+#define GMS_PAIRS_RESIDENT_THREADS 1024
+#endif
 
 namespace gms {
 
@@ -301,7 +306,7 @@ struct PostLayout {
   static constexpr size_t OFF_BAR = (OFF_FLAG + 4 + 15) & ~size_t(15);
   static constexpr size_t BYTES = OFF_BAR + 16;
   // Blocks per SM the register budget is sized for (64 registers at 16 keys per thread).
-  static constexpr int RESIDENT_THREADS = C::IPT <= 8 ? 1536 : (C::KV ? 1024 : GMS_KEYS_RESIDENT_THREADS);
+  static constexpr int RESIDENT_THREADS = C::IPT <= 8 ? 1536 : (C::KV ? GMS_PAIRS_RESIDENT_THREADS : GMS_KEYS_RESIDENT_THREADS);
   static constexpr int MIN_BLOCKS = RESIDENT_THREADS / C::THREADS > 0 ? RESIDENT_THREADS / C::THREADS : 1;
 };
 
