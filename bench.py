@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline time budget")
     p.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
     p.add_argument("--only-batched", action="store_true", help="print only the batched-form summary")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="batched form: keep the built-in tile table instead of autotuning first")
     p.add_argument("--no-serving", action="store_true", help="skip the serving-form measurement")
     p.add_argument("--only-serving", action="store_true", help="print only the serving-form summary")
     p.add_argument("--serve-seconds", type=float, default=3.0)
@@ -186,7 +188,7 @@ def ncu_traffic(kernel: str, n: int):
         return None
 
 
-def run_batched(dev, reps: int = 3):
+def run_batched(dev, reps: int = 3, tune: bool = True):
     """Batched form (4096 segments, log-uniform sizes in [1024, 4194304], seed 7,
     B in {2, 8, 32, 256}, delta or range identifier, key-value) against the plain
     per-call loop over the same segments; returns a summary dict."""
@@ -222,8 +224,9 @@ def run_batched(dev, reps: int = 3):
 
     # Tile shapes per (B, size class) for this device, then the plan from the tuned table.
     t0 = time.perf_counter()
-    gms.autotune(buckets=(2, 8, 32, 256), key_value=(True,), keys_per_trial=1 << 25, reps=5)
-    autotune_s = time.perf_counter() - t0
+    if tune:
+        gms.autotune(buckets=(2, 8, 32, 256), key_value=(True,), keys_per_trial=1 << 25, reps=5)
+    autotune_s = time.perf_counter() - t0 if tune else None
     table = gms.tuning_table()
     chosen = {f"B{B}": [gms.tile_variant_shape(table[(B, True, c)])[2] for c in range(8)] for B in (2, 8, 32, 256)}
     plan = gms.BatchedMultisplit(segs)
@@ -732,7 +735,8 @@ def run_ours(a):
         from gpumultisplit_gb300 import build as gbuild
 
         gbuild.build()
-        out = run_batched(dev) if a.only_batched else run_serving(dev, a.serve_seconds, a.serve_rate)
+        out = (run_batched(dev, tune=not a.no_autotune) if a.only_batched
+               else run_serving(dev, a.serve_seconds, a.serve_rate))
         print(json.dumps(out), flush=True)
         return
     if world > 1:
@@ -924,7 +928,7 @@ def run_ours(a):
     if not a.no_batched:
         del keys, vals, kout, vout
         torch.cuda.empty_cache()
-        line["batched"] = run_batched(dev)
+        line["batched"] = run_batched(dev, tune=not a.no_autotune)
     if not a.no_serving:
         line["serving"] = run_serving(dev, a.serve_seconds, a.serve_rate)
     if rank == 0 and not a.no_cpu_baseline:
