@@ -225,10 +225,13 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
     const uint32_t tile = variant_tile_keys(v);
     d.num_tiles = uint32_t((uint64_t(sg.n) + tile - 1) / tile);
     const uint64_t entries = uint64_t(1u << logb) * d.num_tiles;
-    // Start a new scan group when this segment would push the group's keys past 2^32 - 1.
+    // Start a new scan group when this segment would push the group's keys past
+    // 2^32 - 1.  A group's counts start on a 16-byte boundary (the scan reads
+    // them as 16-byte vectors); the entries skipped for that belong to no group.
     if (group_n + sg.n > 0xFFFFFFFFull) {
       group.m = uint32_t(matrix_total - group.matrix_first);
       b->groups.push_back(group);
+      matrix_total = (matrix_total + 3) & ~uint64_t(3);
       group.matrix_first = uint32_t(matrix_total);
       group_n = 0;
     }

@@ -40,9 +40,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(uint32_t* __restrict
   const uint32_t chunk = s_chunk;
   const uint32_t first = chunk * SCAN_CHUNK + tid * SCAN_IPT;
 
-  // Load 16 consecutive counts per thread.
+  // Load 16 consecutive counts per thread (16-byte vectors when `data` is
+  // 16-byte aligned, which every caller arranges; element loads otherwise).
+  const bool vec = (reinterpret_cast<uintptr_t>(data) & 15u) == 0;
   uint32_t v[SCAN_IPT];
-  if (first + SCAN_IPT <= m) {
+  if (vec && first + SCAN_IPT <= m) {
 #pragma unroll
     for (int k = 0; k < SCAN_IPT / 4; ++k) {
       const uint4 q = *reinterpret_cast<const uint4*>(data + first + 4 * k);
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(uint32_t* __restrict
   out[0] = offset;
 #pragma unroll
   for (int k = 1; k < SCAN_IPT; ++k) out[k] = offset + v[k - 1];
-  if (first + SCAN_IPT <= m) {
+  if (vec && first + SCAN_IPT <= m) {
 #pragma unroll
     for (int k = 0; k < SCAN_IPT / 4; ++k) {
       *reinterpret_cast<uint4*>(data + first + 4 * k) =

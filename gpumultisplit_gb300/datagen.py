@@ -71,8 +71,15 @@ def and4_u32(n: int, seed: int, device="cpu") -> torch.Tensor:
 
 
 def index_values(n: int, device="cpu") -> torch.Tensor:
-    """values = original index (pins value stability)."""
-    return torch.arange(n, dtype=torch.int32, device=device)
+    """values = original index (pins value stability), as uint32 bit patterns in
+    int32 (indices from 2^31 up wrap to negative int32 values)."""
+    if n <= 1 << 31:
+        return torch.arange(n, dtype=torch.int32, device=device)
+    out = torch.empty(n, dtype=torch.int32, device=device)
+    for s in range(0, n, CHUNK):
+        e = min(n, s + CHUNK)
+        out[s:e] = torch.arange(s, e, dtype=torch.int64, device=device).to(torch.int32)  # wraps mod 2^32
+    return out
 
 
 def uniform_unit(n: int, seed: int, device="cpu") -> torch.Tensor:

@@ -81,3 +81,59 @@ def test_sort7_pairs_full_size(gms_lib, dist):
     assert torch.equal(kout, kin[vout.long()])
     same = k[1:] == k[:-1]
     assert bool((vout[1:] > vout[:-1])[same].all()), "not stable"
+
+
+def test_kv_multisplit_beyond_2p31(gms_lib):
+    """n above 2^31 (32-bit index arithmetic, values that do not fit an int32)."""
+    B = 256
+    n = (1 << 31) + 4099
+    kin = datagen.uniform_u32(n, 8, device="cuda")
+    vin = datagen.index_values(n, "cuda")
+    kout, vout = torch.empty_like(kin), torch.empty_like(vin)
+    ctx = gms.multisplit_context(B)
+    gms.multisplit_allocate_key_value(n, ctx)
+    offs = gms.multisplit_key_value(kin, vin, kout, vout, n, ctx, gms.delta_bucket(), multisplit_offset=True)
+    torch.cuda.synchronize()
+    assert gms.read_device_error(ctx) == 0
+    del ctx
+    idx = u64(vout)
+    seen = torch.zeros(n, dtype=torch.int8, device="cuda")
+    seen[idx] = 1
+    assert bool(seen.all()), "values are not a permutation of the indices"
+    del seen
+    assert torch.equal(kout, kin[idx]), "keys did not travel with their values"
+    b = u64(kout) >> 24
+    assert bool((b[1:] >= b[:-1]).all()), "buckets not ascending"
+    assert bool((idx[1:] > idx[:-1])[b[1:] == b[:-1]].all()), "input order not kept inside a bucket"
+    counts = torch.bincount(b, minlength=B)
+    starts = torch.cumsum(counts, 0) - counts
+    assert offs == [int(x) for x in starts.cpu()]
+
+
+def test_batched_scan_groups_beyond_2p32(gms_lib):
+    """A batch whose keys add up to more than 2^32 is scanned in groups; every
+    segment keeps the multisplit properties (key-only: ascending buckets, and
+    per-bucket counts and key sums equal to the input's)."""
+    sizes = [(1 << 31) + 5, 1000, (1 << 31) + 77]
+    buckets = [8, 2, 256]
+    segs, ins, outs = [], [], []
+    for i, (n, B) in enumerate(zip(sizes, buckets)):
+        kin = datagen.uniform_u32(n, 90 + i, device="cuda")
+        kout = torch.empty_like(kin)
+        segs.append(gms.Segment(kin, kout, n, B, gms.delta_bucket()))
+        ins.append(kin)
+        outs.append(kout)
+    plan = gms.BatchedMultisplit(segs)
+    plan.run(use_graph=False)
+    torch.cuda.synchronize()
+    assert plan.device_error() == 0
+    plan.close()
+    for kin, kout, B in zip(ins, outs, buckets):
+        shift = 32 - (B.bit_length() - 1)
+        bi, bo = u64(kin) >> shift, u64(kout) >> shift
+        assert bool((bo[1:] >= bo[:-1]).all())
+        assert torch.equal(torch.bincount(bi, minlength=B), torch.bincount(bo, minlength=B))
+        si = torch.zeros(B, dtype=torch.int64, device="cuda").scatter_add_(0, bi, u64(kin))
+        so = torch.zeros(B, dtype=torch.int64, device="cuda").scatter_add_(0, bo, u64(kout))
+        assert torch.equal(si, so)
+        del bi, bo
