@@ -91,7 +91,7 @@ gms_status generic_histogram(const uint32_t* keys, uint32_t n, uint32_t num_buck
   case L: {                                                                                      \
     static std::atomic<int> per_sm{0};                                                           \
     auto kern = histogram_kernel<L, FunctorPolicy<F, L>>;                                        \
-    const uint32_t grid = persistent_grid(kern, HIST_THREADS, (n + HIST_CHUNK - 1) / HIST_CHUNK, per_sm); \
+    const uint32_t grid = persistent_grid(kern, HIST_THREADS, uint32_t((uint64_t(n) + HIST_CHUNK - 1) / HIST_CHUNK), per_sm); \
     kern<<<grid, HIST_THREADS, 0, s>>>(keys, n, d_hist, f);                                      \
     e = cudaGetLastError();                                                                      \
     break;                                                                                       \
