@@ -354,7 +354,8 @@ gms_status gms_server_destroy(gms_server_t server);
  * zeroes it first, as with the reference's atomicAdd kernels).  Generalises
  * multisplit2_histogram_even_* / _range_* (src/kernels/histogram/multisplit2_histograms.cuh:36-699)
  * to every identifier kind and to any n (the reference needs n to be a whole
- * number of tiles, src/main/main_histogram.cu:76). */
+ * number of tiles, src/main/main_histogram.cu:76).  The bins are int counters
+ * like the reference's; a bin whose count exceeds 2^31 - 1 holds it modulo 2^32. */
 gms_status gms_histogram(const uint32_t* d_key_in, uint32_t n, const gms_bucket_desc* desc, int32_t* d_hist,
                          gms_stream_t stream);
 

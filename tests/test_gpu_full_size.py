@@ -137,3 +137,31 @@ def test_batched_scan_groups_beyond_2p32(gms_lib):
         so = torch.zeros(B, dtype=torch.int64, device="cuda").scatter_add_(0, bo, u64(kout))
         assert torch.equal(si, so)
         del bi, bo
+
+
+def test_largest_n(gms_lib):
+    """n = 2^32 - 1, the largest size the 32-bit interface takes: a histogram
+    and a key-only two-bucket multisplit (checked in chunks to bound memory)."""
+    n = (1 << 32) - 1
+    kin = datagen.uniform_u32(n, 12, device="cuda")
+    hist = torch.zeros(2, dtype=torch.int32, device="cuda")
+    gms.multisplit_histogram(kin, n, hist, 2, gms.delta_bucket())
+    ones = sum(int((kin[s:s + (1 << 28)] < 0).sum()) for s in range(0, n, 1 << 28))  # top bit set
+    # the bins are the reference's int counters: a bin above 2^31 - 1 holds its count mod 2^32
+    h0, h1 = int(hist[0]) & 0xFFFFFFFF, int(hist[1]) & 0xFFFFFFFF
+    assert h1 == ones and h0 + h1 == n
+    kout = torch.empty_like(kin)
+    ctx = gms.multisplit_context(2)
+    gms.multisplit_allocate_key_only(n, ctx)
+    offs = gms.multisplit_key_only(kin, kout, n, ctx, gms.delta_bucket(), multisplit_offset=True)
+    torch.cuda.synchronize()
+    assert gms.read_device_error(ctx) == 0
+    assert offs == [0, n - ones]
+    zeros = n - ones
+    # bucket 0 (top bit clear) first, then bucket 1, and the same keys in each
+    assert bool((kout[:zeros] >= 0).all()) and bool((kout[zeros:] < 0).all())
+    si = so = 0
+    for s in range(0, n, 1 << 28):
+        si += int(u64(kin[s:s + (1 << 28)]).sum())
+        so += int(u64(kout[s:s + (1 << 28)]).sum())
+    assert si == so
