@@ -192,11 +192,12 @@ __device__ __forceinline__ void count_v4(const uint4 (&v)[IPT / 4], Counter& c, 
 // every key's bucket is also stored as one byte at bytes_out[key index].
 template <int THREADS, int IPT, bool WRITE_BYTES = false, class Counter, class Done>
 __device__ __forceinline__ void count_tiles(const uint32_t* __restrict__ keys, uint32_t n, uint32_t first,
-                                            uint32_t stride, Counter& c, Done done, uint8_t* bytes_out = nullptr) {
+                                            uint32_t stride, Counter& c, Done done, uint8_t* bytes_out = nullptr,
+                                            uint32_t last = ~0u) {
   constexpr uint32_t TILE = uint32_t(THREADS) * IPT;
-  const uint32_t num_tiles = uint32_t((uint64_t(n) + TILE - 1) / TILE);
+  const uint32_t num_tiles = min(uint32_t((uint64_t(n) + TILE - 1) / TILE), last);
   const bool vec_ok = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0;
-  const uint32_t full_tiles = vec_ok ? n / TILE : 0u;  // tiles read with vector loads
+  const uint32_t full_tiles = vec_ok ? min(n / TILE, num_tiles) : 0u;  // tiles read with vector loads
   uint4 cur[IPT / 4];
   if (first < full_tiles) load_tile_v4<THREADS, IPT>(keys, first * TILE, cur);
   for (uint32_t tile = first; tile < num_tiles; tile += stride) {
@@ -233,6 +234,13 @@ __device__ __forceinline__ void count_tiles(const uint32_t* __restrict__ keys, u
 // bucket_bytes (identifiers costly to evaluate; may be null): every key's
 // bucket is also stored there as one byte, so the postscan need not evaluate
 // the identifier again.
+//
+// Each block counts a contiguous run of tiles and keeps the counts of
+// PRESCAN_GROUP consecutive tiles in shared memory, then writes them bucket by
+// bucket: a warp stores whole runs of consecutive matrix words (the matrix is
+// bucket-major) instead of one scattered word per bucket and tile.
+constexpr uint32_t PRESCAN_GROUP = 8;
+
 template <class C, class P>
 __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __restrict__ keys, uint32_t n,
                                                              uint32_t num_tiles, uint32_t* __restrict__ counts,
@@ -240,8 +248,10 @@ __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __r
                                                              uint64_t* __restrict__ status, uint32_t num_chunks,
                                                              uint8_t* __restrict__ bucket_bytes) {
   using Counter = KeyCounter<C::LOGB, typename P::Id>;
+  constexpr uint32_t G = PRESCAN_GROUP;
   __shared__ uint32_t s_hist[Counter::smem_words(C::WARPS)];
   __shared__ uint32_t s_split[P::SMEM_WORDS];  // identifier state (RANGE splitters + table)
+  __shared__ uint32_t s_cnt[C::B * G];         // counts of the current group of tiles, bucket-major
 
   const uint32_t tid = threadIdx.x;
 
@@ -257,17 +267,31 @@ __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __r
   Counter counter(P::make(bp, s_split), s_hist);
   counter.clear_shared();
   __syncthreads();
+  // This block's tiles: [first, last), a whole number of groups.
+  const uint32_t per = ((num_tiles + gridDim.x - 1) / gridDim.x + G - 1) / G * G;
+  const uint32_t first = min(blockIdx.x * per, num_tiles);
+  const uint32_t last = min(first + per, num_tiles);
+  auto flush = [&](uint32_t group_first) {
+    __syncthreads();
+    for (uint32_t i = tid; i < C::B * G; i += C::THREADS) {
+      const uint32_t t = group_first + i % G;
+      if (t < last) counts[(i / G) * num_tiles + t] = s_cnt[i];
+    }
+    __syncthreads();
+  };
   auto done = [&](uint32_t tile) {
     const uint32_t total = counter.block_total();
-    if (tid < C::B) counts[tid * num_tiles + tile] = total;
+    const uint32_t g = (tile - first) % G;
+    if (tid < C::B) s_cnt[tid * G + g] = total;
+    if (g == G - 1 || tile + 1 == last) flush(tile - g);
   };
   if constexpr (!P::CHEAP) {
     if (bucket_bytes != nullptr) {
-      count_tiles<C::THREADS, C::IPT, true>(keys, n, blockIdx.x, gridDim.x, counter, done, bucket_bytes);
+      count_tiles<C::THREADS, C::IPT, true>(keys, n, first, 1u, counter, done, bucket_bytes, last);
       return;
     }
   }
-  count_tiles<C::THREADS, C::IPT>(keys, n, blockIdx.x, gridDim.x, counter, done);
+  count_tiles<C::THREADS, C::IPT>(keys, n, first, 1u, counter, done, nullptr, last);
 }
 
 // Shared-memory layout of the postscan for identifier policy P (bytes), and
