@@ -7,6 +7,11 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+// Counts per thread of the look-back scan (a chunk is 256 threads x this).
+#ifndef GMS_SCAN_IPT
+#define GMS_SCAN_IPT 16
+#endif
+
 namespace gms {
 
 // ----------------------------------------------------------------- errors

@@ -50,7 +50,7 @@ inline int size_class(uint32_t n) {
 // Variant the batched form uses for a segment (the tuning table's entry).
 int tuned_variant(int logb, bool kv, uint32_t n);
 
-constexpr uint32_t kScanChunk = 4096;  // SCAN_CHUNK in scan_kernels.cuh
+constexpr uint32_t kScanChunk = 256u * GMS_SCAN_IPT;  // SCAN_CHUNK in scan_kernels.cuh
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 

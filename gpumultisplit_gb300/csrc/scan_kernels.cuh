@@ -13,8 +13,8 @@
 namespace gms {
 
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_IPT = 16;
-constexpr uint32_t SCAN_CHUNK = SCAN_THREADS * SCAN_IPT;  // 4096 counts per chunk
+constexpr int SCAN_IPT = GMS_SCAN_IPT;
+constexpr uint32_t SCAN_CHUNK = SCAN_THREADS * SCAN_IPT;  // counts per chunk
 
 enum : uint32_t { SCAN_FLAG_AGGREGATE = 1u, SCAN_FLAG_PREFIX = 2u };
 
