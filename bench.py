@@ -302,7 +302,10 @@ def run_sweep(a, dev):
     """One JSON line per case, inputs resident in HBM, CUDA events around
     `steps` calls after `warmup` calls, each case's output checked by a
     size-independent property (bucket order + permutation for multisplits,
-    sortedness for sorts, total count for histograms)."""
+    sortedness for sorts, total count for histograms).  Beside each GPU figure,
+    the CPU implementation of the same op (the oracle's restatement of the
+    reference's CPU code: the multisplits on every host thread, the others on
+    one) timed on the first 2^22 keys."""
     import torch
 
     import gpumultisplit_gb300 as gms
@@ -328,10 +331,34 @@ def run_sweep(a, dev):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / steps
 
-    def emit(case, ms, bytes_per_key, check):
+    import oracle
+
+    if not oracle.LIB.exists():
+        oracle.build(with_ref=False)
+    ncpu = os.cpu_count() or 1
+    sample_n = 1 << 22
+
+    def cpu_rate(fn, threads):
+        """CPU implementation of the same op (the oracle: the reference's algorithm)
+        on the first sample_n keys, best of 3; Gkeys/s."""
+        best = None
+        for _ in range(3):
+            t0 = time.perf_counter()
+            fn()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        return {"gkeys": sample_n / best / 1e9, "threads": threads, "sample_keys": sample_n}
+
+    def sample(t):
+        return datagen.as_u32(t[:sample_n])
+
+    def emit(case, ms, bytes_per_key, check, cpu=None):
         line = {"case": case, "n": n, "ms": ms, "gkeys": n / (ms * 1e-3) / 1e9,
                 "algorithmic_bytes_per_key": bytes_per_key,
                 "hbm_frac": bytes_per_key * n / (ms * 1e-3) / 1e9 / peak, "check": check}
+        if cpu is not None:
+            line["cpu"] = cpu
+            line["gpu_vs_cpu"] = line["gkeys"] / cpu["gkeys"]
         print(json.dumps(line), flush=True)
 
     def bucket_ids(x, B, ident_name, spl):
@@ -360,8 +387,12 @@ def run_sweep(a, dev):
                 gms.multisplit_allocate_key_value(n, ctx)
                 kin = inputs[dist]
                 ms = timed(lambda: gms.multisplit_key_value(kin, vals, kout, vout, n, ctx, ident))
+                hk, hv = sample(kin), sample(vals)
+                desc = oracle.Desc(oracle.DELTA if ident_name == "delta" else oracle.RANGE, B,
+                                   splitters=None if spl is None else datagen.as_u32(spl))
                 emit(f"multisplit kv B={B} {dist} {ident_name}", ms, 20,
-                     multisplit_check(kin, kout, vout, B, ident_name, spl))
+                     multisplit_check(kin, kout, vout, B, ident_name, spl),
+                     cpu_rate(lambda: oracle.multisplit_mt(hk, desc, hv, ncpu), ncpu))
                 gms.multisplit_release_memory(ctx)
     for B in (2, 32, 256):
         ctx = gms.multisplit_context(B)
@@ -371,7 +402,9 @@ def run_sweep(a, dev):
         ok = multisplit_check(kin, kout, None, B, "delta", None)
         ok = ok if bool(torch.equal(torch.sort(kout.long() & 0xFFFFFFFF)[0],
                                     torch.sort(kin.long() & 0xFFFFFFFF)[0])) else "FAIL"
-        emit(f"multisplit k B={B} uniform delta", ms, 12, ok)
+        hk = sample(kin)
+        emit(f"multisplit k B={B} uniform delta", ms, 12, ok,
+             cpu_rate(lambda: oracle.multisplit_mt(hk, oracle.Desc(oracle.DELTA, B), None, ncpu), ncpu))
         gms.multisplit_release_memory(ctx)
     # compaction, predicate key & 1
     for kv in (False, True):
@@ -384,8 +417,10 @@ def run_sweep(a, dev):
             gms.compaction_allocate_key_only(n, ctx)
             ms = timed(lambda: gms.compaction_key_only(kin, kout, n, ctx, gms.test_bucket(1)))
         b = kout & 1
+        hk, hv = sample(kin), (sample(vals) if kv else None)
         emit(f"compaction {'kv' if kv else 'k'} key&1 uniform", ms, 20 if kv else 12,
-             "pass" if bool((b[1:] >= b[:-1]).all()) else "FAIL")
+             "pass" if bool((b[1:] >= b[:-1]).all()) else "FAIL",
+             cpu_rate(lambda: oracle.compaction(hk, oracle.Desc(oracle.BITS, 2), hv), 1))
         gms.compaction_release_memory(ctx)
     # 256-bin histograms
     hist = torch.zeros(256, dtype=torch.int32, device=dev)
@@ -393,9 +428,12 @@ def run_sweep(a, dev):
     ms = timed(lambda: gms.multisplit_histogram(kin, n, hist, 256, gms.delta_bucket()))
     hist.zero_()
     gms.multisplit_histogram(kin, n, hist, 256, gms.delta_bucket())
-    emit("histogram 256 bins delta uniform", ms, 4, "pass" if int(hist.sum()) == n else "FAIL")
+    hk = sample(kin)
+    emit("histogram 256 bins delta uniform", ms, 4, "pass" if int(hist.sum()) == n else "FAIL",
+         cpu_rate(lambda: oracle.histogram(hk, oracle.Desc(oracle.DELTA, 256)), 1))
     ms = timed(lambda: gms.histogram_even(kin, n, hist, 256, 0, 0xFFFFFFFF, 256.0 / 2**32))
-    emit("histogram 256 bins even-float uniform", ms, 4, "pass")
+    emit("histogram 256 bins even-float uniform", ms, 4, "pass",
+         cpu_rate(lambda: oracle.histogram(hk, oracle.Desc(oracle.EVEN_FLOAT, 256, inverse_delta=256.0 / 2**32)), 1))
     # sorts
     for bits in (7, 4, 5, 6, 8):
         for dist in (("uniform", "and4") if bits == 7 else ("uniform",)):
@@ -414,8 +452,9 @@ def run_sweep(a, dev):
                 if kv:
                     ok &= bool(torch.equal(kin[vout.long()], kout))
                 passes = {4: 8, 5: 7, 6: 6, 7: 5, 8: 4}[bits]
+                hk, hv = sample(kin), (sample(vals) if kv else None)
                 emit(f"sort {bits}-bit {'kv' if kv else 'k'} {dist}", ms, passes * (20 if kv else 12),
-                     "pass" if ok else "FAIL")
+                     "pass" if ok else "FAIL", cpu_rate(lambda: oracle.sort(hk, hv, bits), 1))
                 gms.multisplit_sort_release_memory(ctx)
 
 
