@@ -417,7 +417,18 @@ void scheduler(gms_server_s* s) {
     progress |= launch_round(s);
     s->stats.arena_peak_bytes = s->requests_arena.peak() + s->rounds_arena.peak();
     if (s->stop && s->queue.empty() && s->active.empty() && s->rounds.empty()) break;
-    if (!progress) s->cv_work.wait_for(lock, std::chrono::microseconds(200));
+    if (progress) continue;
+    if (!s->rounds.empty()) {
+      // A round is on the GPU: poll its event (only this thread touches the
+      // round queue) rather than wait for the host callback, which answers
+      // tens of microseconds later; new submissions are picked up between polls.
+      const cudaEvent_t done = s->rounds.front().done;
+      lock.unlock();
+      for (int i = 0; i < 256 && cudaEventQuery(done) == cudaErrorNotReady; ++i) std::this_thread::yield();
+      lock.lock();
+    } else {
+      s->cv_work.wait_for(lock, std::chrono::microseconds(200));
+    }
   }
 }
 
