@@ -61,8 +61,9 @@ gms_status to_status(cudaError_t e) {
   return GMS_ERROR_CUDA;
 }
 
+// Any bucket count in [2, 256]; *logb = ceil(log2(b)).
 bool log2_buckets(uint32_t b, int* logb) {
-  if (b < 2 || b > 256 || (b & (b - 1)) != 0) return false;
+  if (b < 2 || b > 256) return false;
   int l = 0;
   while ((1u << l) < b) ++l;
   *logb = l;
@@ -200,6 +201,10 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
     const int kind = sg.desc.kind;
     const bool bad_desc = kind < 0 || kind >= NUM_KINDS || (kind == KIND_DIV && sg.desc.param == 0) ||
                           (kind == KIND_RANGE && sg.desc.d_splitters == nullptr);
+    if (kind == KIND_BITS && (sg.desc.num_buckets & (sg.desc.num_buckets - 1)) != 0) {
+      delete b;
+      return GMS_ERROR_UNSUPPORTED_BUCKETS;
+    }
     const bool bad_ptrs = sg.n > 0 && (sg.d_key_in == nullptr || sg.d_key_out == nullptr ||
                                        (kv && sg.d_value_out == nullptr) || (!kv && sg.d_value_out != nullptr));
     if (bad_desc || bad_ptrs) {
@@ -217,6 +222,7 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
     d.bp.lower = sg.desc.lower;
     d.bp.inverse_delta = sg.desc.inverse_delta;
     d.bp.splitters = sg.desc.d_splitters;
+    d.bp.num_buckets = sg.desc.num_buckets;
     const int v = variant >= 0 ? variant : tuned_variant(logb, kv, sg.n);
     if (!variant_valid(v, logb)) {
       delete b;

@@ -19,8 +19,9 @@ gms_status cuda_status(cudaError_t e) {
   return GMS_ERROR_CUDA;
 }
 
+// Any bucket count in [2, 256]; *logb = ceil(log2(b)).
 bool valid_buckets(uint32_t b, int* logb) {
-  if (b < 2 || b > 256 || (b & (b - 1)) != 0) return false;
+  if (b < 2 || b > 256) return false;
   int l = 0;
   while ((1u << l) < b) ++l;
   *logb = l;
@@ -36,8 +37,9 @@ gms_status check_desc(const gms_bucket_desc* d, int* logb) {
   if (d == nullptr) return GMS_ERROR_INVALID_VALUE;
   if (!valid_buckets(d->num_buckets, logb)) return GMS_ERROR_UNSUPPORTED_BUCKETS;
   switch (d->kind) {
+    case GMS_BUCKET_BITS:  // a bit field: the bucket count is a power of two
+      return (d->num_buckets & (d->num_buckets - 1)) == 0 ? GMS_SUCCESS : GMS_ERROR_UNSUPPORTED_BUCKETS;
     case GMS_BUCKET_DELTA:
-    case GMS_BUCKET_BITS:
     case GMS_BUCKET_MASK:
     case GMS_BUCKET_EVEN_FLOAT:
       return GMS_SUCCESS;
@@ -57,6 +59,7 @@ BucketParams to_params(const gms_bucket_desc* d) {
   p.lower = d->lower;
   p.inverse_delta = d->inverse_delta;
   p.splitters = d->d_splitters;
+  p.num_buckets = d->num_buckets;
   return p;
 }
 
@@ -126,10 +129,9 @@ gms_status multisplit_impl(const uint32_t* kin, const uint32_t* vin, uint32_t* k
   return cuda_status(dispatch(desc->kind, c, stages));
 }
 
-// Bucket start offsets: matrix[b * num_tiles] for every b (src/api/multisplit.cuh:143-149).
-gms_status copy_offsets(const void* scratch, uint32_t n, int logb, bool kv, uint32_t* h_offsets,
+// Bucket start offsets: matrix[b * num_tiles] for b < B (src/api/multisplit.cuh:143-149).
+gms_status copy_offsets(const void* scratch, uint32_t n, int logb, uint32_t B, bool kv, uint32_t* h_offsets,
                         cudaStream_t stream) {
-  const uint32_t B = 1u << logb;
   if (n == 0) {
     for (uint32_t b = 0; b < B; ++b) h_offsets[b] = 0;
     return GMS_SUCCESS;
@@ -318,7 +320,7 @@ const char* gms_status_string(gms_status s) {
   switch (s) {
     case GMS_SUCCESS: return "success";
     case GMS_ERROR_INVALID_VALUE: return "invalid value";
-    case GMS_ERROR_UNSUPPORTED_BUCKETS: return "number of buckets must be a power of two in [2, 256]";
+    case GMS_ERROR_UNSUPPORTED_BUCKETS: return "number of buckets must be in [2, 256] (a power of two for bit-field buckets)";
     case GMS_ERROR_SCRATCH_TOO_SMALL: return "scratch buffer too small";
     case GMS_ERROR_CUDA: return "CUDA runtime error";
     case GMS_ERROR_DEVICE_TIMEOUT: return "device-side wait timed out";
@@ -365,7 +367,7 @@ gms_status gms_multisplit_key_only(const uint32_t* d_key_in, uint32_t* d_key_out
   if (st != GMS_SUCCESS || h_offsets == nullptr) return st;
   int logb = 0;
   valid_buckets(desc->num_buckets, &logb);
-  return copy_offsets(d_scratch, n, logb, false, h_offsets, stream);
+  return copy_offsets(d_scratch, n, logb, desc->num_buckets, false, h_offsets, stream);
 }
 
 gms_status gms_multisplit_key_value(const uint32_t* d_key_in, const uint32_t* d_value_in, uint32_t* d_key_out,
@@ -377,7 +379,7 @@ gms_status gms_multisplit_key_value(const uint32_t* d_key_in, const uint32_t* d_
   if (st != GMS_SUCCESS || h_offsets == nullptr) return st;
   int logb = 0;
   valid_buckets(desc->num_buckets, &logb);
-  return copy_offsets(d_scratch, n, logb, true, h_offsets, stream);
+  return copy_offsets(d_scratch, n, logb, desc->num_buckets, true, h_offsets, stream);
 }
 
 gms_status gms_multisplit_prescan(const uint32_t* d_key_in, uint32_t n, const gms_bucket_desc* desc, int key_value,

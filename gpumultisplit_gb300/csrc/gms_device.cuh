@@ -153,13 +153,21 @@ enum BucketKind : int {
   NUM_KINDS = 6
 };
 
+// B = num_buckets may be any count in [2, 256]; the kernels run with
+// 2^LOGB >= B buckets, the ones from B up staying empty.
 struct BucketParams {
   uint32_t shift;
   uint32_t param;
   uint32_t lower;
   float inverse_delta;
   const uint32_t* splitters;  // RANGE only (device memory, B entries)
+  uint32_t num_buckets;       // B
 };
+
+// v modulo b (b in [2, 256]): a mask for powers of two, a division otherwise.
+__device__ __forceinline__ uint32_t reduce_mod(uint32_t v, uint32_t b) {
+  return (b & (b - 1)) == 0 ? (v & (b - 1)) : (v % b);
+}
 
 // RANGE identifiers narrow each search with a table over the key's top
 // RANGE_LUT_BITS bits.  Entry t packs lo(t) | lo(t+1) << 16, where lo(t) is the
@@ -188,22 +196,26 @@ struct Identifier {
 
   __device__ __forceinline__ uint32_t operator()(uint32_t key) const {
     if constexpr (KIND == KIND_DELTA) {
-      // key * B >> 32 with B = 2^LOGB is the top LOGB bits of the key.
-      return key >> (32 - LOGB);
+      // key * B >> 32: the high word of the 64-bit product (the top LOGB bits
+      // of the key when B = 2^LOGB).
+      return __umulhi(key, p.num_buckets);
     } else if constexpr (KIND == KIND_DIV) {
-      return (key / p.param) & (B - 1);
+      return reduce_mod(key / p.param, p.num_buckets);
     } else if constexpr (KIND == KIND_BITS) {
       return (key >> p.shift) & (B - 1);
     } else if constexpr (KIND == KIND_RANGE) {
       // c = number of splitters <= key (upper_bound); bucket = c - 1, which
       // wraps to B-1 when key < s[0].
+      // With B below 2^LOGB the splitter area is padded with 0xFFFFFFFF, so
+      // c is clamped to B.
       if constexpr (B <= RANGE_SCAN_MAX_B) {
         // Few splitters: compare against all of them (same address for every
         // lane, so each load is a broadcast).
         uint32_t c = 0;
 #pragma unroll
         for (uint32_t i = 0; i < B; ++i) c += s_split[i] <= key ? 1u : 0u;
-        return (c - 1u) & (B - 1);
+        c = min(c, p.num_buckets);
+        return c == 0u ? p.num_buckets - 1u : c - 1u;
       } else {
         // The table bounds c to [lo(t), lo(t+1)].  Only keys whose cell holds
         // a splitter load it (a predicated load: lanes in empty cells add no
@@ -224,13 +236,14 @@ struct Identifier {
               hi = mid - 1;
           }
         }
-        return (c - 1u) & (B - 1);
+        c = min(c, p.num_buckets);
+        return c == 0u ? p.num_buckets - 1u : c - 1u;
       }
     } else if constexpr (KIND == KIND_MASK) {
       return (key & p.param) ? 1u : 0u;
     } else {  // KIND_EVEN_FLOAT
       const float x = __fmul_rn(__uint2float_rn(key - p.lower), p.inverse_delta);
-      return __float2uint_rz(x) & (B - 1);
+      return reduce_mod(__float2uint_rz(x), p.num_buckets);
     }
   }
 };
@@ -243,7 +256,7 @@ __device__ __forceinline__ void prepare_identifier(uint32_t* s_split, const Buck
   if constexpr (KIND == KIND_RANGE) {
     constexpr uint32_t B = 1u << LOGB;
     constexpr uint32_t SHIFT = 32 - RANGE_LUT_BITS;
-    for (uint32_t i = threadIdx.x; i < B; i += blockDim.x) s_split[i] = p.splitters[i];
+    for (uint32_t i = threadIdx.x; i < B; i += blockDim.x) s_split[i] = i < p.num_buckets ? p.splitters[i] : ~0u;
     __syncthreads();
     if constexpr (B <= RANGE_SCAN_MAX_B) return;
     uint32_t* lut = s_split + B;

@@ -16,10 +16,13 @@ constexpr int HIST_THREADS = HIST_WARPS * 32;
 constexpr int HIST_IPT = 16;
 constexpr uint32_t HIST_CHUNK = HIST_THREADS * HIST_IPT;
 
-// Persistent grid; block-strided over chunks of HIST_CHUNK keys.
+// Persistent grid; block-strided over chunks of HIST_CHUNK keys.  The counts
+// run over 2^LOGB bins; only the first num_bins (<= 2^LOGB, the caller's
+// array) are written.
 template <int LOGB, class P>
 __global__ void __launch_bounds__(HIST_THREADS) histogram_kernel(const uint32_t* __restrict__ keys, uint32_t n,
-                                                                 int32_t* __restrict__ hist, typename P::Params bp) {
+                                                                 int32_t* __restrict__ hist, typename P::Params bp,
+                                                                 uint32_t num_bins) {
   using Counter = KeyCounter<LOGB, typename P::Id>;
   __shared__ uint32_t s_hist[Counter::smem_words(HIST_WARPS)];
   __shared__ uint32_t s_split[P::SMEM_WORDS];
@@ -29,7 +32,7 @@ __global__ void __launch_bounds__(HIST_THREADS) histogram_kernel(const uint32_t*
   __syncthreads();
   count_tiles<HIST_THREADS, HIST_IPT>(keys, n, blockIdx.x, gridDim.x, counter, [](uint32_t) {});
   const uint32_t total = counter.block_total();
-  if (threadIdx.x < (1u << LOGB) && total) atomicAdd(&hist[threadIdx.x], int32_t(total));
+  if (threadIdx.x < num_bins && total) atomicAdd(&hist[threadIdx.x], int32_t(total));
 }
 
 }  // namespace gms

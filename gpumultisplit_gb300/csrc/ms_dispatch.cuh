@@ -205,7 +205,7 @@ cudaError_t run_histogram_t(const uint32_t* keys, uint32_t n, const BucketParams
   static std::atomic<int> per_sm{0};
   auto kern = histogram_kernel<LOGB, DescPolicy<KIND, LOGB>>;
   const uint32_t grid = persistent_grid(kern, HIST_THREADS, uint32_t((uint64_t(n) + HIST_CHUNK - 1) / HIST_CHUNK), per_sm);
-  kern<<<grid, HIST_THREADS, 0, stream>>>(keys, n, hist, bp);
+  kern<<<grid, HIST_THREADS, 0, stream>>>(keys, n, hist, bp, bp.num_buckets);
   return cudaGetLastError();
 }
 

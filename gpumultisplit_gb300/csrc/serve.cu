@@ -471,7 +471,8 @@ gms_status gms_server_submit(gms_server_t s, const gms_request* r, uint64_t* id)
   if (r->n > 0 && r->d_key_in == nullptr) return GMS_ERROR_INVALID_VALUE;
   if (r->op != GMS_OP_SORT_7BIT) {
     uint32_t b = r->desc.num_buckets;
-    if (b < 2 || b > 256 || (b & (b - 1)) != 0) return GMS_ERROR_UNSUPPORTED_BUCKETS;
+    if (b < 2 || b > 256) return GMS_ERROR_UNSUPPORTED_BUCKETS;
+    if (r->desc.kind == GMS_BUCKET_BITS && (b & (b - 1)) != 0) return GMS_ERROR_UNSUPPORTED_BUCKETS;
     if (r->op == GMS_OP_COMPACTION && b != 2) return GMS_ERROR_INVALID_VALUE;
   }
   if (request_bytes(*r) > s->requests_arena.size()) return GMS_ERROR_SCRATCH_TOO_SMALL;

@@ -35,7 +35,7 @@ typedef struct CUstream_st* gms_stream_t;
 typedef enum gms_status {
   GMS_SUCCESS = 0,
   GMS_ERROR_INVALID_VALUE = 1,       /* null pointer, bad kind, n over capacity ... */
-  GMS_ERROR_UNSUPPORTED_BUCKETS = 2, /* num_buckets not a power of two in [2, 256] */
+  GMS_ERROR_UNSUPPORTED_BUCKETS = 2, /* num_buckets outside [2, 256], or not a power of two for BITS */
   GMS_ERROR_SCRATCH_TOO_SMALL = 3,
   GMS_ERROR_CUDA = 4,                /* a CUDA runtime call failed; see gms_last_cuda_error() */
   GMS_ERROR_DEVICE_TIMEOUT = 5,      /* a bounded device-side wait gave up (read by gms_read_device_error) */
@@ -48,15 +48,21 @@ typedef enum gms_status {
  * log2(B) bits with ballots, src/kernels/bms/bms_prescan.cuh:480-517, so an
  * out-of-range id wraps the same way there).
  *
+ * B may be any count in [2, 256] (the reference takes powers of two only;
+ * for those every kind gives the same buckets as below).  The kernels then
+ * run with the next power of two and leave the buckets from B up empty.
+ * BITS needs a power of two.  Offsets and histograms hold B entries.
+ *
  *  GMS_BUCKET_DELTA       key * B >> 32 (64-bit product): B equal-width key ranges.
- *  GMS_BUCKET_DIV         key / param   (delta_func, README.md:85-91, src/main/main_multisplit.cu:41-47).
+ *  GMS_BUCKET_DIV         (key / param) mod B (delta_func, README.md:85-91, src/main/main_multisplit.cu:41-47).
  *  GMS_BUCKET_BITS        (key >> shift) & (B-1)  (ms_bucket_sort_*bit<shift>, src/api/multisplit_sort.cuh:63-98;
  *                          compaction's test_bucket<1> = key & 1, src/main/main_compaction.cu:26-31).
  *  GMS_BUCKET_RANGE       upper_bound(d_splitters[0..B), key) - 1 (cub::UpperBound on the level array,
  *                          src/kernels/histogram/multisplit2_histograms.cuh:434); keys below
  *                          d_splitters[0] give -1, i.e. bucket B-1 after the wrap.
+ *                          Splitters need not be distinct.
  *  GMS_BUCKET_MASK        (key & param) != 0 (a two-bucket predicate).
- *  GMS_BUCKET_EVEN_FLOAT  (uint32)((float)(key - lower) * inverse_delta), float round-to-nearest
+ *  GMS_BUCKET_EVEN_FLOAT  (uint32)((float)(key - lower) * inverse_delta) mod B, float round-to-nearest
  *                          convert and multiply, truncating saturating convert back
  *                          (src/kernels/histogram/multisplit2_histograms.cuh:60).
  */
@@ -71,7 +77,7 @@ typedef enum gms_bucket_kind {
 
 typedef struct gms_bucket_desc {
   int32_t kind;                /* gms_bucket_kind */
-  uint32_t num_buckets;        /* B: power of two, 2..256 */
+  uint32_t num_buckets;        /* B: 2..256 (a power of two for BITS) */
   uint32_t shift;              /* BITS */
   uint32_t param;              /* DIV: divisor (non-zero); MASK: mask */
   uint32_t lower;              /* EVEN_FLOAT: lower level */
@@ -254,7 +260,8 @@ gms_status gms_batch_create_with_variant(const gms_segment* segments, uint32_t c
  * covers n <= 2^10 for c = 0, 2^(9+c) < n <= 2^(10+c) for 0 < c < 7, and
  * n > 2^16 for c = 7.  A shape is valid for B only when it has at least B
  * threads.  gms_batch_create reads the table, so a change applies to plans
- * created afterwards. */
+ * created afterwards.  The tuning calls take powers of two; a segment whose
+ * B is not one uses the row of the next power of two. */
 #define GMS_NUM_TILE_VARIANTS 4
 #define GMS_NUM_SIZE_CLASSES 8
 gms_status gms_tile_variant_shape(int variant, uint32_t* warps, uint32_t* keys_per_thread, uint32_t* tile_keys);

@@ -46,7 +46,11 @@ namespace dropin {
 inline void allocate(uint32_t n, multisplit_context& c, int key_value) {
   size_t bytes = 0, matrix_off = 0;
   uint32_t tile = 0, tiles = 0;
-  gms_status st = gms_multisplit_scratch_bytes(n, c.num_buckets, key_value, &bytes);
+  // The reference takes powers of two from 2 to 256 only (src/api/multisplit.cuh:91-137);
+  // the C ABI also takes other counts, these headers keep the reference's rule.
+  const uint32_t b = c.num_buckets;
+  gms_status st = (b < 2 || b > 256 || (b & (b - 1)) != 0) ? GMS_ERROR_UNSUPPORTED_BUCKETS : GMS_SUCCESS;
+  if (st == GMS_SUCCESS) st = gms_multisplit_scratch_bytes(n, c.num_buckets, key_value, &bytes);
   if (st == GMS_SUCCESS) st = gms_multisplit_geometry(n, c.num_buckets, key_value, &tile, &tiles, &matrix_off);
   last_status() = st;
   if (st != GMS_SUCCESS) {

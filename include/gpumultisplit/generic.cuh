@@ -92,7 +92,7 @@ gms_status generic_histogram(const uint32_t* keys, uint32_t n, uint32_t num_buck
     static std::atomic<int> per_sm{0};                                                           \
     auto kern = histogram_kernel<L, FunctorPolicy<F, L>>;                                        \
     const uint32_t grid = persistent_grid(kern, HIST_THREADS, uint32_t((uint64_t(n) + HIST_CHUNK - 1) / HIST_CHUNK), per_sm); \
-    kern<<<grid, HIST_THREADS, 0, s>>>(keys, n, d_hist, f);                                      \
+    kern<<<grid, HIST_THREADS, 0, s>>>(keys, n, d_hist, f, num_buckets);                         \
     e = cudaGetLastError();                                                                      \
     break;                                                                                       \
   }

@@ -14,29 +14,31 @@
 #include <stdlib.h>
 #include <string.h>
 
-/* Bucket identifier.  Every kind is reduced modulo B: the reference's GPU
- * kernels decode the bucket from its low log2(B) bits with ballots
- * (src/kernels/bms/bms_prescan.cuh:480-517).
- *   DELTA       key * B >> 32                     (equal-width ranges)
+/* Bucket identifier for B buckets (any B in [2, 256]).  Every kind is reduced
+ * modulo B: the reference's GPU kernels decode the bucket from its low log2(B)
+ * bits with ballots (src/kernels/bms/bms_prescan.cuh:480-517), which is the
+ * same reduction for the powers of two the reference takes.
+ *   DELTA       key * B >> 32                     (equal-width ranges; < B)
  *   DIV         key / param                       (delta_func, src/main/main_multisplit.cu:41-47)
  *   BITS        (key >> shift)                    (ms_bucket_sort_*bit, src/api/multisplit_sort.cuh:63-98)
- *   RANGE       upper_bound(splitters, B, key) - 1 (src/kernels/histogram/multisplit2_histograms.cuh:434)
+ *   RANGE       upper_bound(splitters, B, key) - 1, with -1 read as B-1
+ *                                               (src/kernels/histogram/multisplit2_histograms.cuh:434)
  *   MASK        (key & param) != 0
  *   EVEN_FLOAT  (uint32)((float)(key - lower) * inverse_delta)
  *                                               (src/kernels/histogram/multisplit2_histograms.cuh:60)
  */
 uint32_t oracle_bucket(const oracle_desc* d, uint32_t key) {
-  const uint32_t mask = d->num_buckets - 1u;
+  const uint32_t B = d->num_buckets;
   switch (d->kind) {
     case ORACLE_DELTA:
-      return (uint32_t)(((uint64_t)key * d->num_buckets) >> 32) & mask;
+      return (uint32_t)(((uint64_t)key * B) >> 32);
     case ORACLE_DIV:
-      return (key / d->param) & mask;
+      return (key / d->param) % B;
     case ORACLE_BITS:
-      return (d->shift >= 32u ? 0u : (key >> d->shift)) & mask;
+      return (d->shift >= 32u ? 0u : (key >> d->shift)) % B;
     case ORACLE_RANGE: {
       /* upper_bound: first index whose splitter is > key. */
-      uint32_t lo = 0, hi = d->num_buckets;
+      uint32_t lo = 0, hi = B;
       while (lo < hi) {
         const uint32_t mid = lo + (hi - lo) / 2u;
         if (d->splitters[mid] <= key)
@@ -44,7 +46,7 @@ uint32_t oracle_bucket(const oracle_desc* d, uint32_t key) {
         else
           hi = mid;
       }
-      return (lo - 1u) & mask;
+      return lo == 0u ? B - 1u : lo - 1u;
     }
     case ORACLE_MASK:
       return (key & d->param) ? 1u : 0u;
@@ -60,7 +62,7 @@ uint32_t oracle_bucket(const oracle_desc* d, uint32_t key) {
         b = 0xFFFFFFFFu;
       else
         b = (uint32_t)x;
-      return b & mask;
+      return b % B;
     }
     default:
       return 0u;

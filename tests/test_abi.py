@@ -68,14 +68,22 @@ def test_scratch_and_geometry(gms_lib, B, kv):
 
 
 def test_unsupported_bucket_counts(gms_lib):
-    for B in (0, 1, 3, 12, 257, 512):
+    for B in (0, 1, 257, 512):
         st, _ = scratch_bytes(100, B, 0)
         assert st == _lib.GMS_ERROR_UNSUPPORTED_BUCKETS
+    # any count in [2, 256] is taken (the kernels round it up to a power of two) ...
+    for B in (3, 12, 100, 255):
+        st, nbytes = scratch_bytes(100000, B, 1)
+        assert st == 0 and nbytes == scratch_bytes(100000, 1 << (B - 1).bit_length(), 1)[1]
+    # ... except by a bit-field identifier, whose buckets are a power of two
+    d = gms.bits_bucket(3).desc(12)
+    st = gms_lib.gms_multisplit_key_only(1 << 20, 2 << 20, 10, ctypes.byref(d), 1 << 24, 1 << 30, None, None)
+    assert st == _lib.GMS_ERROR_UNSUPPORTED_BUCKETS
 
 
 def test_argument_checks_before_cuda(gms_lib):
     """These calls fail on their arguments, before any CUDA work."""
-    d = _lib.BucketDesc(kind=_lib.GMS_BUCKET_DELTA, num_buckets=7)
+    d = _lib.BucketDesc(kind=_lib.GMS_BUCKET_DELTA, num_buckets=300)
     assert gms_lib.gms_multisplit_key_only(1 << 20, 2 << 20, 10, ctypes.byref(d), 1 << 24, 1 << 20, None,
                                            None) == _lib.GMS_ERROR_UNSUPPORTED_BUCKETS
     d = _lib.BucketDesc(kind=99, num_buckets=8)

@@ -83,7 +83,9 @@ def test_batched_equals_plain_path_and_replays(gms_lib, oracle_mod):
 def test_batched_rejects_bad_segments(gms_lib):
     k = torch.zeros(10, dtype=torch.int32, device="cuda")
     with pytest.raises(gms.GmsError):
-        gms.BatchedMultisplit([gms.Segment(k, k.clone(), 10, 3, gms.delta_bucket())])
+        gms.BatchedMultisplit([gms.Segment(k, k.clone(), 10, 300, gms.delta_bucket())])
+    with pytest.raises(gms.GmsError):  # bit-field buckets need a power of two
+        gms.BatchedMultisplit([gms.Segment(k, k.clone(), 10, 3, gms.bits_bucket(0))])
     with pytest.raises(gms.GmsError):
         gms.BatchedMultisplit([gms.Segment(k, k.clone(), 10, 8, gms.delta_func(0))])
 

@@ -157,7 +157,9 @@ def test_invalid_requests_rejected(gms_lib):
     server = gms.Server(arena_bytes=1 << 24)
     k = torch.zeros(16, dtype=torch.int32, device="cuda")
     with pytest.raises(gms.GmsError):
-        server.submit("multisplit", k, None, 16, 3, gms.delta_bucket())
+        server.submit("multisplit", k, None, 16, 300, gms.delta_bucket())
+    with pytest.raises(gms.GmsError):  # bit-field buckets need a power of two
+        server.submit("multisplit", k, None, 16, 3, gms.bits_bucket(0))
     with pytest.raises(gms.GmsError):
         server.submit("compaction", k, None, 16, 4, gms.delta_bucket())
     server.close()

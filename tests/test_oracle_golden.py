@@ -153,3 +153,25 @@ def test_partial_key_sort_oracle(oracle_mod, begin, end, digit):
     assert np.array_equal(ko, keys[order])
     with pytest.raises(ValueError):
         oracle_mod.sort_bits(keys, vals, 5, 4, 8)
+
+
+def test_oracle_buckets_any_count(oracle_mod):
+    """Bucket counts that are not powers of two: every id is below B, and the
+    identifiers agree with their definitions."""
+    o = oracle_mod
+    keys = datagen.as_u32(datagen.uniform_u32(4000, 31))
+    keys[:3] = [0, 0xFFFFFFFF, 0x80000000]
+    for B in (3, 5, 12, 100, 255):
+        k64 = keys.astype(np.uint64)
+        assert np.array_equal(o.buckets(keys, o.Desc(o.DELTA, B)), (k64 * B >> 32).astype(np.uint32))
+        assert np.array_equal(o.buckets(keys, o.Desc(o.DIV, B, param=77777)), (keys // 77777) % B)
+        spl = np.concatenate([[0], np.sort(datagen.as_u32(datagen.uniform_u32(B - 1, B)))]).astype(np.uint32)
+        ub = np.searchsorted(spl, keys, side="right").astype(np.int64) - 1
+        assert np.array_equal(o.buckets(keys, o.Desc(o.RANGE, B, splitters=spl)), np.where(ub < 0, B - 1, ub))
+        assert o.buckets(keys, o.Desc(o.EVEN_FLOAT, B, inverse_delta=B / 2**32)).max() < B
+        if o.ref_available():
+            vals = np.arange(keys.size, dtype=np.uint32)
+            d = o.Desc(o.RANGE, B, splitters=spl)
+            ko, vo, _ = o.multisplit(keys, d, vals)
+            rk, rv = o.ref_multisplit(keys, d, vals)
+            assert np.array_equal(ko, rk) and np.array_equal(vo, rv)
