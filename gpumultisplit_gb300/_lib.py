@@ -41,6 +41,20 @@ class BucketDesc(ctypes.Structure):
     ]
 
 
+class BucketDesc64(ctypes.Structure):
+    """gms_bucket_desc64 (identifiers for 64-bit keys, or 32-bit keys with 64-bit values)."""
+
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("num_buckets", ctypes.c_uint32),
+        ("shift", ctypes.c_uint32),
+        ("inverse_delta", ctypes.c_float),
+        ("param", ctypes.c_uint64),
+        ("lower", ctypes.c_uint64),
+        ("d_splitters", ctypes.c_void_p),
+    ]
+
+
 class GmsError(RuntimeError):
     def __init__(self, status: int, what: str, cuda_error: int = 0):
         self.status = status
@@ -58,6 +72,7 @@ _SZ = ctypes.c_size_t
 _PU32 = ctypes.POINTER(ctypes.c_uint32)
 _PSZ = ctypes.POINTER(ctypes.c_size_t)
 _PDESC = ctypes.POINTER(BucketDesc)
+_PDESC64 = ctypes.POINTER(BucketDesc64)
 
 # name -> argtypes (every function returns gms_status as int32 unless listed in _RESTYPES)
 _PROTOS = {
@@ -79,6 +94,10 @@ _PROTOS = {
     "gms_sort_bits_scratch_bytes": [_U32, _I32, _I32, _I32, _I32, _PSZ],
     "gms_sort_bits_key_only": [_P, _P, _U32, _I32, _I32, _I32, _P, _SZ, _P],
     "gms_sort_bits_key_value": [_P, _P, _P, _P, _U32, _I32, _I32, _I32, _P, _SZ, _P],
+    "gms_multisplit_wide_scratch_bytes": [_U32, _U32, _I32, _I32, _PSZ],
+    "gms_multisplit_wide": [_P, _P, _P, _P, _U32, _I32, _I32, _PDESC64, _P, _SZ, _PU32, _P],
+    "gms_sort_wide_scratch_bytes": [_U32, _I32, _I32, _I32, _I32, _I32, _PSZ],
+    "gms_sort_wide": [_P, _P, _P, _P, _U32, _I32, _I32, _I32, _I32, _I32, _P, _SZ, _P],
     "gms_sort_7bit_scratch_bytes": [_U32, _I32, _PSZ],
     "gms_sort_7bit_key_only": [_P, _P, _U32, _P, _SZ, _P],
     "gms_sort_7bit_key_value": [_P, _P, _P, _P, _U32, _P, _SZ, _P],

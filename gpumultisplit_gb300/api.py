@@ -32,7 +32,7 @@ import ctypes
 from dataclasses import dataclass
 
 from . import _lib
-from ._lib import BucketDesc, check
+from ._lib import BucketDesc, BucketDesc64, check
 
 # ---------------------------------------------------------------- helpers
 
@@ -45,7 +45,7 @@ def _ptr(x, elem_bytes: int | None = 4) -> int | None:
         return x
     if hasattr(x, "data_ptr"):
         if elem_bytes is not None and x.element_size() != elem_bytes:
-            raise TypeError("multisplit buffers hold 32-bit elements")
+            raise TypeError(f"this buffer must hold {8 * elem_bytes}-bit elements")
         if not x.is_cuda:
             raise TypeError("multisplit buffers must be CUDA tensors")
         return x.data_ptr()
@@ -82,6 +82,11 @@ class BucketIdentifier:
     def desc(self, num_buckets: int) -> BucketDesc:  # pragma: no cover - abstract
         raise NotImplementedError
 
+    def desc64(self, num_buckets: int) -> BucketDesc64:  # pragma: no cover - abstract
+        """The gms_bucket_desc64 of this identifier (64-bit parameters), for
+        multisplit_wide / 64-bit keys."""
+        raise NotImplementedError
+
 
 @dataclass
 class delta_bucket(BucketIdentifier):
@@ -89,6 +94,9 @@ class delta_bucket(BucketIdentifier):
 
     def desc(self, num_buckets):
         return BucketDesc(kind=_lib.GMS_BUCKET_DELTA, num_buckets=num_buckets)
+
+    def desc64(self, num_buckets):
+        return BucketDesc64(kind=_lib.GMS_BUCKET_DELTA, num_buckets=num_buckets)
 
 
 @dataclass
@@ -100,6 +108,9 @@ class delta_func(BucketIdentifier):
     def desc(self, num_buckets):
         return BucketDesc(kind=_lib.GMS_BUCKET_DIV, num_buckets=num_buckets, param=int(self.delta))
 
+    def desc64(self, num_buckets):
+        return BucketDesc64(kind=_lib.GMS_BUCKET_DIV, num_buckets=num_buckets, param=int(self.delta))
+
 
 @dataclass
 class bits_bucket(BucketIdentifier):
@@ -109,6 +120,9 @@ class bits_bucket(BucketIdentifier):
 
     def desc(self, num_buckets):
         return BucketDesc(kind=_lib.GMS_BUCKET_BITS, num_buckets=num_buckets, shift=int(self.shift))
+
+    def desc64(self, num_buckets):
+        return BucketDesc64(kind=_lib.GMS_BUCKET_BITS, num_buckets=num_buckets, shift=int(self.shift))
 
 
 def ms_bucket_sort_4bit(shift: int) -> bits_bucket:
@@ -137,6 +151,9 @@ class mask_bucket(BucketIdentifier):
     def desc(self, num_buckets):
         return BucketDesc(kind=_lib.GMS_BUCKET_MASK, num_buckets=num_buckets, param=int(self.mask))
 
+    def desc64(self, num_buckets):
+        return BucketDesc64(kind=_lib.GMS_BUCKET_MASK, num_buckets=num_buckets, param=int(self.mask))
+
 
 class range_bucket(BucketIdentifier):
     """bucket = upper_bound(splitters, key) - 1 over B sorted splitters (device
@@ -147,6 +164,11 @@ class range_bucket(BucketIdentifier):
 
     def desc(self, num_buckets):
         return BucketDesc(kind=_lib.GMS_BUCKET_RANGE, num_buckets=num_buckets, d_splitters=_ptr(self.d_splitters))
+
+    def desc64(self, num_buckets):
+        # the splitters have the keys' width (int32 for 32-bit keys, int64 for 64-bit keys)
+        return BucketDesc64(kind=_lib.GMS_BUCKET_RANGE, num_buckets=num_buckets,
+                            d_splitters=_ptr(self.d_splitters, None))
 
 
 @dataclass
@@ -160,6 +182,10 @@ class even_float_bucket(BucketIdentifier):
     def desc(self, num_buckets):
         return BucketDesc(kind=_lib.GMS_BUCKET_EVEN_FLOAT, num_buckets=num_buckets, lower=int(self.lower),
                           inverse_delta=float(self.inverse_delta))
+
+    def desc64(self, num_buckets):
+        return BucketDesc64(kind=_lib.GMS_BUCKET_EVEN_FLOAT, num_buckets=num_buckets, lower=int(self.lower),
+                            inverse_delta=float(self.inverse_delta))
 
 
 # -------------------------------------------------------------- multisplit
@@ -288,6 +314,71 @@ def multisplit_stages(d_key_in, d_value_in, d_key_out, d_value_out, num_elements
                                       num_elements, ctypes.byref(desc), scratch, nbytes, s), "multisplit_postscan")
     if events:
         events[3].record()
+
+
+# ------------------------------------------------ 64-bit keys and values
+
+
+def _elem_bytes(t) -> int:
+    return 0 if t is None else int(t.element_size())
+
+
+def multisplit_wide_allocate(num_elements: int, context: multisplit_context, key_bytes: int,
+                             value_bytes: int = 0) -> None:
+    """Scratch for multisplit_wide with keys of key_bytes (4 or 8) and values of
+    value_bytes (0 for key-only, 4 or 8)."""
+    nbytes = ctypes.c_size_t()
+    check(_lib.load().gms_multisplit_wide_scratch_bytes(num_elements, context.num_buckets, int(key_bytes),
+                                                        int(value_bytes), ctypes.byref(nbytes)),
+          "multisplit_wide_allocate")
+    context.temp_storage_bytes = nbytes.value
+    context.d_temp_storage = _alloc_scratch(nbytes.value)
+    context.widths = (int(key_bytes), int(value_bytes))
+
+
+def multisplit_wide(d_key_in, d_key_out, num_elements: int, context: multisplit_context,
+                    bucket_identifier: BucketIdentifier, d_value_in=None, d_value_out=None, multisplit_offset=None,
+                    stream=None):
+    """Stable multisplit with 32- or 64-bit keys and 32- or 64-bit values (the
+    element widths of the tensors, int32 or int64; the same as at allocation).
+    Same order and offsets as multisplit_key_value; the identifier is applied
+    to the key's full width."""
+    kb, vb = _elem_bytes(d_key_in), _elem_bytes(d_value_in)
+    if getattr(context, "widths", (kb, vb)) != (kb, vb):
+        raise ValueError(f"context allocated for widths {context.widths}, called with {(kb, vb)}")
+    desc = bucket_identifier.desc64(context.num_buckets)
+    offs = _offsets_buffer(context.num_buckets) if multisplit_offset is not None else None
+    check(_lib.load().gms_multisplit_wide(_ptr(d_key_in, kb), _ptr(d_value_in, vb or None), _ptr(d_key_out, kb),
+                                          _ptr(d_value_out, vb or None), num_elements, kb, vb, ctypes.byref(desc),
+                                          _scratch(context),
+                                          context.temp_storage_bytes, offs, _stream(stream)), "multisplit_wide")
+    return _export_offsets(offs, multisplit_offset)
+
+
+def multisplit_sort_wide_allocate(n_elements: int, context, key_bytes: int, value_bytes: int = 0,
+                                  begin_bit: int = 0, end_bit: int | None = None, digit_bits: int = 8) -> None:
+    """Scratch for a stable sort of key_bytes-wide keys (with value_bytes-wide
+    values) by key bits [begin_bit, end_bit) (end_bit defaults to the key width)."""
+    end = 8 * int(key_bytes) if end_bit is None else int(end_bit)
+    nbytes = ctypes.c_size_t()
+    check(_lib.load().gms_sort_wide_scratch_bytes(n_elements, int(key_bytes), int(value_bytes), int(begin_bit), end,
+                                                  int(digit_bits), ctypes.byref(nbytes)),
+          "multisplit_sort_wide_allocate")
+    context.temp_storage_bytes = nbytes.value
+    context.d_temp_storage = _alloc_scratch(max(nbytes.value, 256))
+    context.wide = (int(key_bytes), int(value_bytes), int(begin_bit), end, int(digit_bits))
+
+
+def multisplit_sort_wide(d_key_in, d_key_out, n_elements: int, context, d_value_in=None, d_value_out=None,
+                         stream=None) -> None:
+    """Stable sort by the key bit range given at allocation; keys and values are
+    int32 or int64 tensors of the widths given there."""
+    kb, vb, b, e, d = context.wide
+    if (_elem_bytes(d_key_in), _elem_bytes(d_value_in)) != (kb, vb):
+        raise ValueError("tensor widths differ from the allocation")
+    check(_lib.load().gms_sort_wide(_ptr(d_key_in, kb), _ptr(d_key_out, kb), _ptr(d_value_in, vb or None),
+                                    _ptr(d_value_out, vb or None), n_elements, kb, vb, b, e, d, _scratch(context),
+                                    context.temp_storage_bytes, _stream(stream)), "multisplit_sort_wide")
 
 
 def read_device_error(context, stream=None) -> int:

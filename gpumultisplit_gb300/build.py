@@ -35,9 +35,11 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build gpumultisplit_gb300")
 
 
-# inst_batch.cu is compiled once per (identifier kind, tile variant); the
-# counts match NUM_KINDS in gms_device.cuh and kNumTileVariants in ms_host.h.
+# inst_batch.cu is compiled once per (identifier kind, tile variant) and
+# inst_wide.cu once per identifier kind; the counts match NUM_KINDS in
+# gms_device.cuh and kNumTileVariants in ms_host.h.
 BATCH_INST = "inst_batch.cu"
+WIDE_INST = "inst_wide.cu"
 NUM_KINDS = 6
 NUM_TILE_VARIANTS = 4
 
@@ -54,6 +56,9 @@ def _units() -> list[tuple[Path, str, list[str]]]:
             for k in range(NUM_KINDS):
                 for v in range(NUM_TILE_VARIANTS):
                     units.append((s, f"{s.stem}_k{k}_v{v}", [f"-DGMS_INST_KIND={k}", f"-DGMS_INST_VARIANT={v}"]))
+        elif s.name == WIDE_INST:
+            for k in range(NUM_KINDS):
+                units.append((s, f"{s.stem}_k{k}", [f"-DGMS_INST_KIND={k}"]))
         else:
             units.append((s, s.stem, []))
     return units

@@ -88,11 +88,11 @@ cudaError_t dispatch_hist(int kind, const uint32_t* keys, uint32_t n, int logb, 
   }
 }
 
-bool overlaps(const void* a, const void* b, uint32_t n) {
+// Whether [a, a + n*elem_a) and [b, b + n*elem_b) share a byte.
+bool overlaps(const void* a, const void* b, uint32_t n, size_t elem_a = 4, size_t elem_b = 4) {
   if (a == nullptr || b == nullptr || n == 0) return false;
   const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
-  const uintptr_t len = uintptr_t(n) * 4u;
-  return x < y + len && y < x + len;
+  return x < y + uintptr_t(n) * elem_b && y < x + uintptr_t(n) * elem_a;
 }
 
 // Shared body of the multisplit entry points (stage mask selects the kernels).
@@ -131,12 +131,12 @@ gms_status multisplit_impl(const uint32_t* kin, const uint32_t* vin, uint32_t* k
 
 // Bucket start offsets: matrix[b * num_tiles] for b < B (src/api/multisplit.cuh:143-149).
 gms_status copy_offsets(const void* scratch, uint32_t n, int logb, uint32_t B, bool kv, uint32_t* h_offsets,
-                        cudaStream_t stream) {
+                        cudaStream_t stream, int kw = 1, int vw = 1) {
   if (n == 0) {
     for (uint32_t b = 0; b < B; ++b) h_offsets[b] = 0;
     return GMS_SUCCESS;
   }
-  const Geometry g = make_geometry(n, logb, kv);
+  const Geometry g = make_geometry(n, logb, kv, kw, vw);
   const auto* matrix = static_cast<const unsigned char*>(scratch) + g.off_matrix;
   cudaError_t e = cudaMemcpy2DAsync(h_offsets, sizeof(uint32_t), matrix, size_t(g.num_tiles) * 4, sizeof(uint32_t),
                                     B, cudaMemcpyDeviceToHost, stream);
@@ -149,8 +149,8 @@ gms_status copy_offsets(const void* scratch, uint32_t n, int logb, uint32_t B, b
 // (shift, buckets) per pass, least significant digit first.
 struct SortSchedule {
   int passes;
-  uint32_t shift[8];
-  uint32_t buckets[8];
+  uint32_t shift[16];
+  uint32_t buckets[16];
 };
 
 bool sort_schedule(int digit_bits, SortSchedule* s) {
@@ -164,10 +164,11 @@ bool sort_schedule(int digit_bits, SortSchedule* s) {
   }
 }
 
-// Partial-key schedule: digits of digit_bits bits from begin_bit up to end_bit,
-// the last one narrower when the range is not a whole number of digits.
-bool bit_schedule(int begin_bit, int end_bit, int digit_bits, SortSchedule* s) {
-  if (digit_bits < 4 || digit_bits > 8 || begin_bit < 0 || end_bit > 32 || begin_bit > end_bit) return false;
+// Partial-key schedule: digits of digit_bits bits from begin_bit up to end_bit
+// (at most key_bits), the last one narrower when the range is not a whole
+// number of digits.
+bool bit_schedule(int begin_bit, int end_bit, int digit_bits, SortSchedule* s, int key_bits = 32) {
+  if (digit_bits < 4 || digit_bits > 8 || begin_bit < 0 || end_bit > key_bits || begin_bit > end_bit) return false;
   s->passes = 0;
   for (int sh = begin_bit; sh < end_bit; sh += digit_bits) {
     const int w = end_bit - sh < digit_bits ? end_bit - sh : digit_bits;
@@ -267,6 +268,197 @@ gms_status compaction_impl(const uint32_t* kin, const uint32_t* vin, uint32_t* k
                                   cudaMemcpyDeviceToHost, stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
   return cuda_status(e);
+}
+
+// ------------------------------------------------ 64-bit keys and values
+// key_bytes 4 or 8; value_bytes 0 (key-only), 4 or 8.
+bool valid_widths(int key_bytes, int value_bytes) {
+  return (key_bytes == 4 || key_bytes == 8) && (value_bytes == 0 || value_bytes == 4 || value_bytes == 8);
+}
+
+// The 32-bit descriptor of a 64-bit one, for 32-bit keys (whose parameters
+// must fit in 32 bits; the splitters are 32-bit keys).
+gms_status narrow_desc(const gms_bucket_desc64* d, gms_bucket_desc* out) {
+  if (d == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (d->param > 0xFFFFFFFFull || d->lower > 0xFFFFFFFFull) return GMS_ERROR_INVALID_VALUE;
+  *out = gms_bucket_desc{};
+  out->kind = d->kind;
+  out->num_buckets = d->num_buckets;
+  out->shift = d->shift;
+  out->param = uint32_t(d->param);
+  out->lower = uint32_t(d->lower);
+  out->inverse_delta = d->inverse_delta;
+  out->d_splitters = static_cast<const uint32_t*>(d->d_splitters);
+  return GMS_SUCCESS;
+}
+
+gms_status check_desc64(const gms_bucket_desc64* d, int* logb) {
+  if (d == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (!valid_buckets(d->num_buckets, logb)) return GMS_ERROR_UNSUPPORTED_BUCKETS;
+  switch (d->kind) {
+    case GMS_BUCKET_BITS:
+      if ((d->num_buckets & (d->num_buckets - 1)) != 0) return GMS_ERROR_UNSUPPORTED_BUCKETS;
+      return d->shift < 64 ? GMS_SUCCESS : GMS_ERROR_INVALID_VALUE;
+    case GMS_BUCKET_DELTA:
+    case GMS_BUCKET_MASK:
+    case GMS_BUCKET_EVEN_FLOAT:
+      return GMS_SUCCESS;
+    case GMS_BUCKET_DIV:
+      return d->param != 0 ? GMS_SUCCESS : GMS_ERROR_INVALID_VALUE;
+    case GMS_BUCKET_RANGE:
+      return d->d_splitters != nullptr ? GMS_SUCCESS : GMS_ERROR_INVALID_VALUE;
+    default:
+      return GMS_ERROR_INVALID_VALUE;
+  }
+}
+
+BucketParams64 to_params64(const gms_bucket_desc64* d) {
+  BucketParams64 p{};
+  p.param = d->param;
+  p.lower = d->lower;
+  p.splitters = static_cast<const uint64_t*>(d->d_splitters);
+  p.inverse_delta = d->inverse_delta;
+  p.shift = d->shift;
+  p.num_buckets = d->num_buckets;
+  return p;
+}
+
+cudaError_t dispatch_wide(int kind, const MsCallWide& c, int stages) {
+  switch (kind) {
+    case KIND_DELTA: return run_multisplit_wide<KIND_DELTA>(c, stages);
+    case KIND_DIV: return run_multisplit_wide<KIND_DIV>(c, stages);
+    case KIND_BITS: return run_multisplit_wide<KIND_BITS>(c, stages);
+    case KIND_RANGE: return run_multisplit_wide<KIND_RANGE>(c, stages);
+    case KIND_MASK: return run_multisplit_wide<KIND_MASK>(c, stages);
+    case KIND_EVEN_FLOAT: return run_multisplit_wide<KIND_EVEN_FLOAT>(c, stages);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// Scratch bytes a wide multisplit needs: 64-bit keys always keep their
+// bucket bytes, 32-bit keys as for gms_multisplit_scratch_bytes.
+size_t wide_required_bytes(const Geometry& g, int key_bytes) { return key_bytes == 8 ? g.bytes_full : g.bytes; }
+
+// Any element widths.  32-bit keys with 32-bit (or no) values take the
+// 32-bit path; everything else the 64-bit instances.
+gms_status multisplit_wide_impl(const void* kin, const void* vin, void* kout, void* vout, uint32_t n, int key_bytes,
+                                int value_bytes, const gms_bucket_desc64* desc, void* scratch, size_t scratch_bytes,
+                                cudaStream_t stream) {
+  if (!valid_widths(key_bytes, value_bytes)) return GMS_ERROR_INVALID_VALUE;
+  const bool kv = value_bytes != 0;
+  if (key_bytes == 4 && value_bytes != 8) {
+    gms_bucket_desc d32;
+    gms_status st = narrow_desc(desc, &d32);
+    if (st != GMS_SUCCESS) return st;
+    return multisplit_impl(static_cast<const uint32_t*>(kin), static_cast<const uint32_t*>(vin),
+                           static_cast<uint32_t*>(kout), static_cast<uint32_t*>(vout), n, &d32, kv, scratch,
+                           scratch_bytes, STAGE_ALL, stream);
+  }
+  int logb = 0;
+  gms_status st = key_bytes == 8 ? check_desc64(desc, &logb) : GMS_SUCCESS;
+  gms_bucket_desc d32{};
+  if (key_bytes == 4) {
+    st = narrow_desc(desc, &d32);
+    if (st == GMS_SUCCESS) st = check_desc(&d32, &logb);
+  }
+  if (st != GMS_SUCCESS) return st;
+  if (n == 0) return GMS_SUCCESS;
+  if (scratch == nullptr || (reinterpret_cast<uintptr_t>(scratch) & 255u) != 0) return GMS_ERROR_INVALID_VALUE;
+  const size_t kb = size_t(key_bytes), vb = size_t(value_bytes);
+  auto misaligned = [](const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) != 0; };
+  if (kin == nullptr || kout == nullptr || misaligned(kin, kb) || misaligned(kout, kb) ||
+      overlaps(kin, kout, n, kb, kb))
+    return GMS_ERROR_INVALID_VALUE;
+  if (kv && (vin == nullptr || vout == nullptr || misaligned(vin, vb) || misaligned(vout, vb) ||
+             overlaps(vin, vout, n, vb, vb) || overlaps(kout, vout, n, kb, vb)))
+    return GMS_ERROR_INVALID_VALUE;
+  const int kw = key_bytes / 4, vw = kv ? value_bytes / 4 : 1;
+  const Geometry g = make_geometry(n, logb, kv, kw, vw);
+  if (scratch_bytes < wide_required_bytes(g, key_bytes)) return GMS_ERROR_SCRATCH_TOO_SMALL;
+  MsCallWide c;
+  c.kin = kin;
+  c.vin = kv ? vin : nullptr;
+  c.kout = kout;
+  c.vout = kv ? vout : nullptr;
+  c.n = n;
+  c.logb = logb;
+  c.kv = kv;
+  c.kw = kw;
+  c.vw = vw;
+  c.scratch = static_cast<unsigned char*>(scratch);
+  c.stream = stream;
+  if (key_bytes == 8) {
+    c.bp64 = to_params64(desc);
+    c.bucket_bytes = c.scratch + g.off_buckets;
+  } else {
+    c.bp = to_params(&d32);
+    if (kind_keeps_bucket_bytes(desc->kind) && scratch_bytes >= g.bytes_full) c.bucket_bytes = c.scratch + g.off_buckets;
+  }
+  return cuda_status(dispatch_wide(desc->kind, c, STAGE_ALL));
+}
+
+// Layout of a wide sort's scratch: the multisplit's scratch (largest over the
+// passes), then ping-pong keys and values.
+SortLayout sort_layout_wide(uint32_t n, int key_bytes, int value_bytes, const SortSchedule& sch) {
+  SortLayout L;
+  L.ms_bytes = 0;
+  if (sch.passes == 0) {
+    L.off_keys = L.off_vals = L.bytes = 0;
+    return L;
+  }
+  const bool kv = value_bytes != 0;
+  for (int p = 0; p < sch.passes; ++p) {
+    int logb = 0;
+    valid_buckets(sch.buckets[p], &logb);
+    const Geometry g = make_geometry(n, logb, kv, key_bytes / 4, kv ? value_bytes / 4 : 1);
+    const size_t b = wide_required_bytes(g, key_bytes);
+    L.ms_bytes = b > L.ms_bytes ? b : L.ms_bytes;
+  }
+  L.off_keys = align_up(L.ms_bytes, 256);
+  L.off_vals = align_up(L.off_keys + size_t(n) * key_bytes, 256);
+  L.bytes = kv ? align_up(L.off_vals + size_t(n) * value_bytes, 256) : L.off_vals;
+  return L;
+}
+
+// Stable LSD sort by key bits [begin_bit, end_bit) through wide multisplits,
+// ping-ponging like sort_run so the last pass lands in the output.
+gms_status sort_wide_run(const void* kin, void* kout, const void* vin, void* vout, uint32_t n, int key_bytes,
+                         int value_bytes, const SortSchedule& sch, void* scratch, size_t scratch_bytes,
+                         cudaStream_t stream) {
+  const bool kv = value_bytes != 0;
+  if (n == 0) return GMS_SUCCESS;
+  if (kin == nullptr || kout == nullptr || (scratch == nullptr && sch.passes > 0)) return GMS_ERROR_INVALID_VALUE;
+  if (kv && (vin == nullptr || vout == nullptr)) return GMS_ERROR_INVALID_VALUE;
+  const SortLayout L = sort_layout_wide(n, key_bytes, value_bytes, sch);
+  if (scratch_bytes < L.bytes) return GMS_ERROR_SCRATCH_TOO_SMALL;
+  const size_t kb = size_t(n) * key_bytes, vb = size_t(n) * value_bytes;
+  if (sch.passes == 0) {
+    if (overlaps(kin, kout, n, key_bytes, key_bytes) || (kv && overlaps(vin, vout, n, value_bytes, value_bytes)))
+      return GMS_ERROR_INVALID_VALUE;
+    cudaError_t e = cudaMemcpyAsync(kout, kin, kb, cudaMemcpyDeviceToDevice, stream);
+    if (e == cudaSuccess && kv) e = cudaMemcpyAsync(vout, vin, vb, cudaMemcpyDeviceToDevice, stream);
+    return cuda_status(e);
+  }
+  auto* base = static_cast<unsigned char*>(scratch);
+  void* tk = base + L.off_keys;
+  void* tv = kv ? base + L.off_vals : nullptr;
+  const void* ki = kin;
+  const void* vi = vin;
+  for (int p = 0; p < sch.passes; ++p) {
+    const bool to_out = ((sch.passes - 1 - p) % 2) == 0;
+    void* ko = to_out ? kout : tk;
+    void* vo = to_out ? vout : tv;
+    gms_bucket_desc64 d{};
+    d.kind = GMS_BUCKET_BITS;
+    d.num_buckets = sch.buckets[p];
+    d.shift = sch.shift[p];
+    gms_status st = multisplit_wide_impl(ki, kv ? vi : nullptr, ko, kv ? vo : nullptr, n, key_bytes, value_bytes,
+                                         &d, scratch, L.ms_bytes, stream);
+    if (st != GMS_SUCCESS) return st;
+    ki = ko;
+    vi = vo;
+  }
+  return GMS_SUCCESS;
 }
 
 }  // namespace
@@ -507,6 +699,49 @@ gms_status gms_histogram_range(const uint32_t* d_key_in, uint32_t n, int32_t* d_
   d.num_buckets = num_bins;
   d.d_splitters = d_levels;
   return gms_histogram(d_key_in, n, &d, d_hist, stream);
+}
+
+gms_status gms_multisplit_wide_scratch_bytes(uint32_t max_elements, uint32_t num_buckets, int key_bytes,
+                                             int value_bytes, size_t* bytes) {
+  int logb = 0;
+  if (bytes == nullptr || !valid_widths(key_bytes, value_bytes)) return GMS_ERROR_INVALID_VALUE;
+  if (!valid_buckets(num_buckets, &logb)) return GMS_ERROR_UNSUPPORTED_BUCKETS;
+  const bool kv = value_bytes != 0;
+  *bytes = make_geometry(max_elements, logb, kv, key_bytes / 4, kv ? value_bytes / 4 : 1).bytes_full;
+  return GMS_SUCCESS;
+}
+
+gms_status gms_multisplit_wide(const void* d_key_in, const void* d_value_in, void* d_key_out, void* d_value_out,
+                               uint32_t n, int key_bytes, int value_bytes, const gms_bucket_desc64* desc,
+                               void* d_scratch, size_t scratch_bytes, uint32_t* h_offsets, gms_stream_t stream) {
+  gms_status st = multisplit_wide_impl(d_key_in, d_value_in, d_key_out, d_value_out, n, key_bytes, value_bytes, desc,
+                                       d_scratch, scratch_bytes, stream);
+  if (st != GMS_SUCCESS || h_offsets == nullptr) return st;
+  int logb = 0;
+  valid_buckets(desc->num_buckets, &logb);
+  const bool kv = value_bytes != 0;
+  return copy_offsets(d_scratch, n, logb, desc->num_buckets, kv, h_offsets, stream, key_bytes / 4,
+                      kv ? value_bytes / 4 : 1);
+}
+
+gms_status gms_sort_wide_scratch_bytes(uint32_t max_elements, int key_bytes, int value_bytes, int begin_bit,
+                                       int end_bit, int digit_bits, size_t* bytes) {
+  SortSchedule sch;
+  if (bytes == nullptr || !valid_widths(key_bytes, value_bytes) ||
+      !bit_schedule(begin_bit, end_bit, digit_bits, &sch, 8 * key_bytes))
+    return GMS_ERROR_INVALID_VALUE;
+  *bytes = sort_layout_wide(max_elements, key_bytes, value_bytes, sch).bytes;
+  return GMS_SUCCESS;
+}
+
+gms_status gms_sort_wide(const void* d_key_in, void* d_key_out, const void* d_value_in, void* d_value_out, uint32_t n,
+                         int key_bytes, int value_bytes, int begin_bit, int end_bit, int digit_bits, void* d_scratch,
+                         size_t scratch_bytes, gms_stream_t stream) {
+  SortSchedule sch;
+  if (!valid_widths(key_bytes, value_bytes) || !bit_schedule(begin_bit, end_bit, digit_bits, &sch, 8 * key_bytes))
+    return GMS_ERROR_INVALID_VALUE;
+  return sort_wide_run(d_key_in, d_key_out, d_value_in, d_value_out, n, key_bytes, value_bytes, sch, d_scratch,
+                       scratch_bytes, stream);
 }
 
 }  // extern "C"

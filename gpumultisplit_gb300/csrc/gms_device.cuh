@@ -305,6 +305,115 @@ struct DescPolicy {
   __device__ __forceinline__ static Id make(const Params& p, const uint32_t* s) { return Id{p, s}; }
 };
 
+// ------------------------------------------------ 64-bit key identifiers
+// The same six kinds over 64-bit keys.  They run in the prescan only: the
+// postscan of 64-bit keys always reads the bucket bytes the prescan stored.
+struct BucketParams64 {
+  uint64_t param;               // DIV: divisor; MASK: mask
+  uint64_t lower;               // EVEN_FLOAT: lower level
+  const uint64_t* splitters;    // RANGE: B sorted splitters (device memory)
+  float inverse_delta;          // EVEN_FLOAT
+  uint32_t shift;               // BITS: 0..63
+  uint32_t num_buckets;         // B
+};
+
+// Shared words of a 64-bit identifier: RANGE keeps 2^LOGB splitters (two
+// words each) and, above RANGE_SCAN_MAX_B, a table over the key's top
+// RANGE_LUT_BITS bits, entry t = lo(t) | lo(t+1) << 16 as for 32-bit keys.
+template <int KIND, int LOGB>
+__host__ __device__ constexpr uint32_t identifier64_smem_words() {
+  return KIND != KIND_RANGE ? 1u
+                            : ((1u << LOGB) <= RANGE_SCAN_MAX_B ? 2u * (1u << LOGB)
+                                                                 : 2u * (1u << LOGB) + RANGE_LUT_CELLS);
+}
+
+template <int KIND, int LOGB>
+struct Identifier64 {
+  static constexpr uint32_t B = 1u << LOGB;
+  BucketParams64 p;
+  const uint32_t* s_split;
+
+  __device__ __forceinline__ uint32_t operator()(uint64_t key) const {
+    if constexpr (KIND == KIND_DELTA) {
+      // key * B >> 64: the high word of the 128-bit product.
+      return uint32_t(__umul64hi(key, uint64_t(p.num_buckets)));
+    } else if constexpr (KIND == KIND_DIV) {
+      const uint64_t q = key / p.param;
+      return (p.num_buckets & (p.num_buckets - 1)) == 0 ? uint32_t(q) & (p.num_buckets - 1)
+                                                        : uint32_t(q % p.num_buckets);
+    } else if constexpr (KIND == KIND_BITS) {
+      return uint32_t(key >> p.shift) & (B - 1);
+    } else if constexpr (KIND == KIND_RANGE) {
+      const uint64_t* s = reinterpret_cast<const uint64_t*>(s_split);
+      uint32_t c = 0, hi = B;
+      if constexpr (B > RANGE_SCAN_MAX_B) {
+        const uint32_t e = s_split[2 * B + uint32_t(key >> (64 - RANGE_LUT_BITS))];
+        c = e & 0xFFFFu;
+        hi = e >> 16;
+      }
+      // upper_bound over s[c, hi): the first splitter above the key.
+      while (c < hi) {
+        const uint32_t mid = (c + hi) >> 1;
+        if (s[mid] <= key)
+          c = mid + 1;
+        else
+          hi = mid;
+      }
+      c = min(c, p.num_buckets);
+      return c == 0u ? p.num_buckets - 1u : c - 1u;
+    } else if constexpr (KIND == KIND_MASK) {
+      return (key & p.param) ? 1u : 0u;
+    } else {  // KIND_EVEN_FLOAT
+      const float x = __fmul_rn(__ull2float_rn(key - p.lower), p.inverse_delta);
+      return reduce_mod(__float2uint_rz(x), p.num_buckets);
+    }
+  }
+};
+
+// Fill a 64-bit identifier's shared area (RANGE only; padded to 2^LOGB
+// splitters with the largest key).  All threads call; a barrier must follow.
+template <int KIND, int LOGB>
+__device__ __forceinline__ void prepare_identifier64(uint32_t* s_split, const BucketParams64& p) {
+  if constexpr (KIND == KIND_RANGE) {
+    constexpr uint32_t B = 1u << LOGB;
+    uint64_t* s = reinterpret_cast<uint64_t*>(s_split);
+    for (uint32_t i = threadIdx.x; i < B; i += blockDim.x) s[i] = i < p.num_buckets ? p.splitters[i] : ~0ull;
+    __syncthreads();
+    if constexpr (B <= RANGE_SCAN_MAX_B) return;
+    uint32_t* lut = s_split + 2 * B;
+    for (uint32_t t = threadIdx.x; t < RANGE_LUT_CELLS; t += blockDim.x) {
+      // lo(v) = number of splitters below v, for the first keys of cells t and t + 1.
+      auto below = [&](uint64_t v) {
+        uint32_t lo = 0, hi = B;
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (s[mid] < v)
+            lo = mid + 1;
+          else
+            hi = mid;
+        }
+        return lo;
+      };
+      const uint32_t a = below(uint64_t(t) << (64 - RANGE_LUT_BITS));
+      const uint32_t b = t + 1 == RANGE_LUT_CELLS ? B : below(uint64_t(t + 1) << (64 - RANGE_LUT_BITS));
+      lut[t] = a | (b << 16);
+    }
+  }
+}
+
+template <int KIND, int LOGB>
+struct DescPolicy64 {
+  using Params = BucketParams64;
+  using Id = Identifier64<KIND, LOGB>;
+  static constexpr bool CHEAP = false;  // 64-bit keys always keep their buckets as bytes
+  static constexpr bool USES_SMEM = KIND == KIND_RANGE;
+  static constexpr uint32_t SMEM_WORDS = identifier64_smem_words<KIND, LOGB>();
+  __device__ __forceinline__ static void prepare(uint32_t* s, const Params& p) {
+    prepare_identifier64<KIND, LOGB>(s, p);
+  }
+  __device__ __forceinline__ static Id make(const Params& p, const uint32_t* s) { return Id{p, s}; }
+};
+
 // A user functor (operator() on a 32-bit key, returning the bucket); its
 // value is reduced modulo B like every other identifier.
 template <class F, int LOGB>

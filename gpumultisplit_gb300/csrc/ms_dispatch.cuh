@@ -53,19 +53,56 @@ inline uint32_t persistent_grid(Kernel k, int threads, uint32_t work, std::atomi
 // identifiers that are costly to evaluate, the prescan stores every key's
 // bucket there and the postscan reads it instead of evaluating the identifier
 // a second time; the prescan and postscan of one multisplit must agree on it.
-template <class P, int LOGB, bool KV>
-cudaError_t launch_multisplit(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n,
-                              const typename P::Params& params, unsigned char* scratch, int stages,
+//
+// KW / VW: 32-bit words per key / value.  64-bit keys (KW = 2) are identified
+// by the prescan only, which stores every key's bucket in bucket_bytes (then
+// required); their postscan reads those bytes.
+template <int W>
+using ElemT = std::conditional_t<W == 2, uint64_t, uint32_t>;
+
+template <class P, int LOGB, bool KV, int KW = 1, int VW = 1>
+cudaError_t launch_multisplit(const ElemT<KW>* kin, const ElemT<VW>* vin, ElemT<KW>* kout, ElemT<VW>* vout,
+                              uint32_t n, const typename P::Params& params, unsigned char* scratch, int stages,
                               cudaStream_t stream, uint8_t* bucket_bytes = nullptr) {
   if constexpr (P::CHEAP) bucket_bytes = nullptr;
-  using S = TileShape<LOGB, KV>;
-  using C = TileCfg<LOGB, S::WARPS, S::IPT, KV>;
-  const Geometry g = make_geometry(n, LOGB, KV);
+  using S = TileShape<LOGB, KV, KW, VW>;
+  using C = TileCfg<LOGB, S::WARPS, S::IPT, KV, KW, VW>;
+  const Geometry g = make_geometry(n, LOGB, KV, KW, VW);
   if (g.num_tiles == 0) return cudaSuccess;
   auto* hdr = reinterpret_cast<ScratchHeader*>(scratch);
   auto* status = reinterpret_cast<uint64_t*>(scratch + g.off_status);
   auto* matrix = reinterpret_cast<uint32_t*>(scratch + g.off_matrix);
 
+  if constexpr (KW == 2) {
+    if (bucket_bytes == nullptr) return cudaErrorInvalidValue;
+    if (stages & STAGE_PRESCAN) {
+      static std::atomic<int> per_sm{0};
+      auto kern = prescan64_kernel<C, P>;
+      const uint32_t grid = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm);
+      kern<<<grid, C::THREADS, 0, stream>>>(kin, n, g.num_tiles, matrix, params, hdr, status, g.num_chunks,
+                                            bucket_bytes);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    if (stages & STAGE_SCAN) {
+      cudaError_t e = run_scan(matrix, g.m, status, hdr, stream);
+      if (e != cudaSuccess) return e;
+    }
+    if (stages & STAGE_POSTSCAN) {
+      static std::atomic<uint64_t> smem_done{0};
+      static std::atomic<int> per_sm{0};
+      auto kern = postscan_kernel<C, P, true>;
+      constexpr size_t smem = PostLayout<C, P, true>::BYTES;
+      cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
+      if (e != cudaSuccess) return e;
+      const uint32_t wave = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
+      const uint32_t dist = (GMS_PREFETCH_WAVES * wave) / 4u;
+      kern<<<g.num_tiles, C::THREADS, smem, stream>>>(kin, vin, kout, vout, n, g.num_tiles, matrix, params, hdr,
+                                                        dist, bucket_bytes);
+      return cudaGetLastError();
+    }
+    return cudaSuccess;
+  } else {
   if (stages & STAGE_PRESCAN) {
     static std::atomic<int> per_sm{0};
     auto kern = prescan_kernel<C, P>;
@@ -123,6 +160,7 @@ cudaError_t launch_multisplit(const uint32_t* kin, const uint32_t* vin, uint32_t
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+  }
 }
 
 template <int KIND, int LOGB, bool KV>
@@ -149,6 +187,48 @@ cudaError_t run_multisplit_kv(const MsCall& c, int stages) {
 template <int KIND>
 cudaError_t run_multisplit(const MsCall& c, int stages) {
   return c.kv ? run_multisplit_kv<KIND, true>(c, stages) : run_multisplit_kv<KIND, false>(c, stages);
+}
+
+// 64-bit elements: (key words, value words) = (1, 2), (2, 0), (2, 1), (2, 2).
+template <int KIND, int LOGB, bool KV, int KW, int VW>
+cudaError_t run_multisplit_wide_t(const MsCallWide& c, int stages) {
+  using K = ElemT<KW>;
+  using V = ElemT<VW>;
+  const K* kin = static_cast<const K*>(c.kin);
+  const V* vin = static_cast<const V*>(c.vin);
+  K* kout = static_cast<K*>(c.kout);
+  V* vout = static_cast<V*>(c.vout);
+  if constexpr (KW == 2)
+    return launch_multisplit<DescPolicy64<KIND, LOGB>, LOGB, KV, KW, VW>(kin, vin, kout, vout, c.n, c.bp64,
+                                                                           c.scratch, stages, c.stream,
+                                                                           c.bucket_bytes);
+  else
+    return launch_multisplit<DescPolicy<KIND, LOGB>, LOGB, KV, KW, VW>(kin, vin, kout, vout, c.n, c.bp, c.scratch,
+                                                                         stages, c.stream, c.bucket_bytes);
+}
+
+template <int KIND, int LOGB>
+cudaError_t run_multisplit_wide_l(const MsCallWide& c, int stages) {
+  if (c.kw == 1 && c.kv && c.vw == 2) return run_multisplit_wide_t<KIND, LOGB, true, 1, 2>(c, stages);
+  if (c.kw == 2 && !c.kv) return run_multisplit_wide_t<KIND, LOGB, false, 2, 1>(c, stages);
+  if (c.kw == 2 && c.kv && c.vw == 1) return run_multisplit_wide_t<KIND, LOGB, true, 2, 1>(c, stages);
+  if (c.kw == 2 && c.kv && c.vw == 2) return run_multisplit_wide_t<KIND, LOGB, true, 2, 2>(c, stages);
+  return cudaErrorInvalidValue;  // 32-bit keys and values take run_multisplit
+}
+
+template <int KIND>
+cudaError_t run_multisplit_wide(const MsCallWide& c, int stages) {
+  switch (c.logb) {
+    case 1: return run_multisplit_wide_l<KIND, 1>(c, stages);
+    case 2: return run_multisplit_wide_l<KIND, 2>(c, stages);
+    case 3: return run_multisplit_wide_l<KIND, 3>(c, stages);
+    case 4: return run_multisplit_wide_l<KIND, 4>(c, stages);
+    case 5: return run_multisplit_wide_l<KIND, 5>(c, stages);
+    case 6: return run_multisplit_wide_l<KIND, 6>(c, stages);
+    case 7: return run_multisplit_wide_l<KIND, 7>(c, stages);
+    case 8: return run_multisplit_wide_l<KIND, 8>(c, stages);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 template <int KIND, int LOGB, bool KV, int V>
@@ -231,5 +311,7 @@ cudaError_t run_histogram(const uint32_t* keys, uint32_t n, int logb, const Buck
   template cudaError_t gms::run_multisplit<K>(const gms::MsCall&, int);                                \
   template cudaError_t gms::run_histogram<K>(const uint32_t*, uint32_t, int, const gms::BucketParams&, \
                                              int32_t*, cudaStream_t);
+
+#define GMS_INSTANTIATE_WIDE(K) template cudaError_t gms::run_multisplit_wide<K>(const gms::MsCallWide&, int);
 
 #define GMS_INSTANTIATE_BATCH(K, V) template cudaError_t gms::run_batch_class_v<K, V>(const gms::BatchClassLaunch&, int);

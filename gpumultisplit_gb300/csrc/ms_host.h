@@ -16,10 +16,16 @@ namespace gms {
 // 4096-key tiles of 8 warps x 16 keys per thread measured best on GB300 for
 // every B (16 x 8 and 16 x 16 shapes, and 8 x 8, were slower); at B = 256 the
 // count matrix is then 1 byte per key.
-template <int LOGB, bool KV>
+//
+// With 64-bit keys or values (KW / VW = 32-bit words per key / value) a tile
+// of more than 8 bytes per key is halved to 2048 keys, so that the staged
+// tile still leaves room for five or six blocks per SM.
+constexpr int tile_ipt(bool kv, int kw, int vw) { return 4 * kw + (kv ? 4 * vw : 0) <= 8 ? 16 : 8; }
+
+template <int LOGB, bool KV, int KW = 1, int VW = 1>
 struct TileShape {
   static constexpr int WARPS = 8;
-  static constexpr int IPT = 16;
+  static constexpr int IPT = tile_ipt(KV, KW, VW);
 };
 
 uint32_t tile_keys(int logb, bool kv);
@@ -68,9 +74,10 @@ struct Geometry {
   size_t bytes_full = 0;    // bytes plus the bucket bytes (what gms_multisplit_scratch_bytes reports)
 };
 
-inline Geometry make_geometry(uint32_t n, int logb, bool kv) {
+// kw / vw: 32-bit words per key / value (2 for 64-bit elements).
+inline Geometry make_geometry(uint32_t n, int logb, bool kv, int kw = 1, int vw = 1) {
   Geometry g;
-  g.tile = tile_keys(logb, kv);
+  g.tile = (kw == 1 && (vw == 1 || !kv)) ? tile_keys(logb, kv) : 8u * 32u * uint32_t(tile_ipt(kv, kw, vw));
   g.num_tiles = uint32_t((uint64_t(n) + g.tile - 1) / g.tile);
   g.m = (1u << logb) * g.num_tiles;
   g.num_chunks = (g.m + kScanChunk - 1) / kScanChunk;
@@ -108,6 +115,30 @@ struct MsCall {
 // identifier kind in inst_*.cu.
 template <int KIND>
 cudaError_t run_multisplit(const MsCall& c, int stages);
+
+// A multisplit with 64-bit keys (kw = 2) or 64-bit values (vw = 2).  32-bit
+// keys are identified with bp, 64-bit keys with bp64; 64-bit keys need
+// bucket_bytes (n bytes in the scratch).
+struct MsCallWide {
+  const void* kin = nullptr;
+  const void* vin = nullptr;
+  void* kout = nullptr;
+  void* vout = nullptr;
+  uint32_t n = 0;
+  int logb = 1;
+  bool kv = false;
+  int kw = 1;
+  int vw = 1;
+  BucketParams bp{};
+  BucketParams64 bp64{};
+  unsigned char* scratch = nullptr;  // laid out as make_geometry(n, logb, kv, kw, vw)
+  cudaStream_t stream = nullptr;
+  uint8_t* bucket_bytes = nullptr;
+};
+
+// Defined per identifier kind in inst_wide.cu (compiled once per kind).
+template <int KIND>
+cudaError_t run_multisplit_wide(const MsCallWide& c, int stages);
 
 // Histogram of keys[0..n) into hist[0..2^logb), accumulated with atomics.
 template <int KIND>

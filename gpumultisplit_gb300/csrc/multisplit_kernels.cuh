@@ -45,8 +45,9 @@
 
 namespace gms {
 
-// Tile geometry of one (B, key/value) instance.
-template <int LOGB_, int WARPS_, int IPT_, bool KV_>
+// Tile geometry of one (B, key/value, element widths) instance.  KW and VW
+// are the 32-bit words of a key and of a value (1 or 2): 64-bit elements.
+template <int LOGB_, int WARPS_, int IPT_, bool KV_, int KW_ = 1, int VW_ = 1>
 struct TileCfg {
   static constexpr int LOGB = LOGB_;
   static constexpr uint32_t B = 1u << LOGB_;
@@ -55,6 +56,12 @@ struct TileCfg {
   static constexpr int IPT = IPT_;  // keys per thread
   static constexpr uint32_t TILE = THREADS * IPT_;
   static constexpr bool KV = KV_;
+  static constexpr int KW = KW_;
+  static constexpr int VW = VW_;
+  static constexpr bool WIDE = KW_ == 2 || (KV_ && VW_ == 2);  // any 64-bit element
+  using KT = std::conditional_t<KW_ == 2, uint64_t, uint32_t>;
+  using VT = std::conditional_t<VW_ == 2, uint64_t, uint32_t>;
+  static_assert((KW_ == 1 || KW_ == 2) && (VW_ == 1 || VW_ == 2), "elements are 32 or 64 bits");
   static constexpr uint32_t WB = B < 32 ? 32 : B;  // row width of the per-warp count table
   // Words per count-table entry: {peer bitmap, count} pairs when the bitmap
   // peer search is used (B > 32), else the count alone.
@@ -294,6 +301,97 @@ __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __r
   count_tiles<C::THREADS, C::IPT>(keys, n, first, 1u, counter, done, nullptr, last);
 }
 
+// ------------------------------------------------ prescan, 64-bit keys
+// The prescan for 64-bit keys: the same tiles, counts, group flush and scan
+// reset as prescan_kernel, and every key's bucket is always stored as one
+// byte (the 64-bit postscan reads them instead of the keys' identifier).
+// In a full tile, thread t loads keys 2(k*THREADS + t) and the next one as one
+// 16-byte vector, for k < IPT/2; the next tile's vectors are in flight while
+// the current tile is counted.
+template <int THREADS, int IPT>
+__device__ __forceinline__ void load_tile64(const uint64_t* __restrict__ keys, uint32_t base,
+                                            uint4 (&v)[IPT / 2]) {
+#pragma unroll
+  for (int k = 0; k < IPT / 2; ++k)
+    v[k] = ld_nc_v4(reinterpret_cast<const uint32_t*>(keys + base + (uint32_t(k) * THREADS + threadIdx.x) * 2u));
+}
+
+template <class C, class P>
+__global__ void __launch_bounds__(C::THREADS) prescan64_kernel(const uint64_t* __restrict__ keys, uint32_t n,
+                                                               uint32_t num_tiles, uint32_t* __restrict__ counts,
+                                                               typename P::Params bp, ScratchHeader* hdr,
+                                                               uint64_t* __restrict__ status, uint32_t num_chunks,
+                                                               uint8_t* __restrict__ bucket_bytes) {
+  using Counter = KeyCounter<C::LOGB, typename P::Id>;
+  constexpr uint32_t G = PRESCAN_GROUP;
+  constexpr uint32_t TILE = C::TILE;
+  constexpr int NV = C::IPT / 2;
+  __shared__ uint32_t s_hist[Counter::smem_words(C::WARPS)];
+  __shared__ __align__(16) uint32_t s_split[P::SMEM_WORDS];  // RANGE: 64-bit splitters + table
+  __shared__ uint32_t s_cnt[C::B * G];
+
+  const uint32_t tid = threadIdx.x;
+  for (uint32_t i = blockIdx.x * C::THREADS + tid; i < num_chunks; i += gridDim.x * C::THREADS) status[i] = 0ull;
+  if (blockIdx.x == 0 && tid == 0) {
+    hdr->error = 0u;
+    hdr->error_info = 0u;
+    hdr->ticket = 0u;
+  }
+
+  P::prepare(s_split, bp);
+  Counter counter(P::make(bp, s_split), s_hist);
+  counter.clear_shared();
+  __syncthreads();
+  const uint32_t per = ((num_tiles + gridDim.x - 1) / gridDim.x + G - 1) / G * G;
+  const uint32_t first = min(blockIdx.x * per, num_tiles);
+  const uint32_t last = min(first + per, num_tiles);
+  auto flush = [&](uint32_t group_first) {
+    __syncthreads();
+    for (uint32_t i = tid; i < C::B * G; i += C::THREADS) {
+      const uint32_t t = group_first + i % G;
+      if (t < last) counts[(i / G) * num_tiles + t] = s_cnt[i];
+    }
+    __syncthreads();
+  };
+
+  const bool vec_ok = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0;
+  const uint32_t full_tiles = vec_ok ? min(n / TILE, last) : 0u;
+  uint4 cur[NV];
+  if (first < full_tiles) load_tile64<C::THREADS, C::IPT>(keys, first * TILE, cur);
+  for (uint32_t tile = first; tile < last; ++tile) {
+    uint4 nxt[NV];
+    if (tile + 1 < full_tiles) load_tile64<C::THREADS, C::IPT>(keys, (tile + 1) * TILE, nxt);
+    const uint32_t base = tile * TILE;
+    if (tile < full_tiles) {
+      uint16_t* out = reinterpret_cast<uint16_t*>(bucket_bytes + base);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        const uint32_t b0 = counter.ident(uint64_t(cur[k].x) | (uint64_t(cur[k].y) << 32));
+        const uint32_t b1 = counter.ident(uint64_t(cur[k].z) | (uint64_t(cur[k].w) << 32));
+        counter.template add_bucket<0>(b0, true);
+        counter.template add_bucket<1>(b1, true);
+        out[uint32_t(k) * C::THREADS + tid] = uint16_t(b0 | (b1 << 8));
+      }
+    } else {
+      const uint32_t cnt = min(TILE, n - base);
+#pragma unroll 4
+      for (int k = 0; k < C::IPT; ++k) {
+        const uint32_t i = uint32_t(k) * C::THREADS + tid;
+        const bool valid = i < cnt;
+        const uint32_t b = counter.ident(valid ? keys[base + i] : 0ull);
+        counter.add_bucket(b, valid);
+        if (valid) bucket_bytes[base + i] = uint8_t(b);
+      }
+    }
+    const uint32_t total = counter.block_total();
+    const uint32_t g = (tile - first) % G;
+    if (tid < C::B) s_cnt[tid * G + g] = total;
+    if (g == G - 1 || tile + 1 == last) flush(tile - g);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) cur[k] = nxt[k];
+  }
+}
+
 // Shared-memory layout of the postscan for identifier policy P (bytes), and
 // what phase 3 writes at each key's bucket-sorted position:
 //   R_KEYS       the key (key-only, identifier cheap to recompute): phase 4
@@ -311,13 +409,17 @@ template <class C, class P, bool GIVEN = false>
 struct PostLayout {
   static constexpr bool CHEAP = P::CHEAP;
   static_assert(!GIVEN || !P::CHEAP, "given bucket bytes are only used for costly identifiers");
-  static constexpr int MODE = C::KV ? (CHEAP ? R_INDEX16 : R_INDEX16_B) : (CHEAP ? R_KEYS : R_KEYS_B);
+  static_assert(C::KW == 1 || GIVEN, "64-bit keys take their buckets from the prescan's bytes");
+  // Keys are reordered through a 16-bit index whenever values come along or
+  // keys are 64 bits wide (a sorted copy of the keys would take more room).
+  static constexpr int MODE =
+      (C::KV || C::KW == 2) ? (CHEAP ? R_INDEX16 : R_INDEX16_B) : (CHEAP ? R_KEYS : R_KEYS_B);
   static constexpr bool INDEXED = MODE == R_INDEX16 || MODE == R_INDEX16_B;
   static constexpr bool BUCKET_BYTES = MODE == R_KEYS_B || MODE == R_INDEX16_B;
   using WhT = std::conditional_t<C::WS == 2, uint32_t, uint16_t>;
   static constexpr size_t OFF_K = 0;
-  static constexpr size_t OFF_V = OFF_K + C::TILE * 4;
-  static constexpr size_t OFF_R = OFF_V + (C::KV ? C::TILE * 4 : 0);
+  static constexpr size_t OFF_V = OFF_K + size_t(C::TILE) * sizeof(typename C::KT);
+  static constexpr size_t OFF_R = OFF_V + (C::KV ? size_t(C::TILE) * sizeof(typename C::VT) : 0);
   static constexpr size_t R_BYTES = size_t(C::TILE) * (INDEXED ? 2 : 4);
   static constexpr size_t OFF_RB = OFF_R + R_BYTES;  // bucket bytes
   static constexpr size_t OFF_WH = (OFF_RB + (BUCKET_BYTES ? C::TILE : 0) + 15) & ~size_t(15);
@@ -331,7 +433,12 @@ struct PostLayout {
   static constexpr size_t BYTES = OFF_BAR + 16;
   // Blocks per SM the register budget is sized for (64 registers at 16 keys per thread).
   static constexpr int RESIDENT_THREADS = C::IPT <= 8 ? 1536 : (C::KV ? GMS_PAIRS_RESIDENT_THREADS : GMS_KEYS_RESIDENT_THREADS);
-  static constexpr int MIN_BLOCKS = RESIDENT_THREADS / C::THREADS > 0 ? RESIDENT_THREADS / C::THREADS : 1;
+  static constexpr int THREAD_BLOCKS = RESIDENT_THREADS / C::THREADS > 0 ? RESIDENT_THREADS / C::THREADS : 1;
+  // With 64-bit elements shared memory bounds the blocks per SM first
+  // (228 KB per SM, 1 KB of it reserved per block).
+  static constexpr int SMEM_BLOCKS = int((228u * 1024u) / (BYTES + 1024u));
+  static constexpr int MIN_BLOCKS =
+      C::WIDE ? (SMEM_BLOCKS < THREAD_BLOCKS ? (SMEM_BLOCKS > 0 ? SMEM_BLOCKS : 1) : THREAD_BLOCKS) : THREAD_BLOCKS;
 };
 
 // Peer mask (lanes of this warp whose key in this slot has bucket b) from
@@ -356,18 +463,20 @@ __device__ __forceinline__ uint32_t peers_by_ballot(uint32_t b) {
 // input order) by the caller, so the identifier is not evaluated; phase 3
 // overwrites that area with the buckets in sorted order.
 template <class C, class P, bool FULL, bool GIVEN = false>
-__device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
-                                              uint32_t cnt, uint32_t goff, const typename P::Params& bp,
+__device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout, typename C::VT* __restrict__ vout,
+                                              uint32_t n, uint32_t cnt, uint32_t goff, const typename P::Params& bp,
                                               ScratchHeader* hdr, unsigned char* smem) {
   using L = PostLayout<C, P, GIVEN>;
   using WhT = typename L::WhT;
+  using KT = typename C::KT;
+  using VT = typename C::VT;
   constexpr uint32_t B = C::B;
   constexpr int LOGB = C::LOGB;
   constexpr int IPT = C::IPT;
   constexpr uint32_t WB = C::WB;
   constexpr uint32_t WS = C::WS;
-  uint32_t* s_k = reinterpret_cast<uint32_t*>(smem + L::OFF_K);
-  uint32_t* s_v = reinterpret_cast<uint32_t*>(smem + L::OFF_V);
+  KT* s_k = reinterpret_cast<KT*>(smem + L::OFF_K);
+  VT* s_v = reinterpret_cast<VT*>(smem + L::OFF_V);
   uint32_t* s_r = reinterpret_cast<uint32_t*>(smem + L::OFF_R);
   uint8_t* s_rb = reinterpret_cast<uint8_t*>(smem + L::OFF_RB);
   WhT* s_wh = reinterpret_cast<WhT*>(smem + L::OFF_WH);
@@ -381,6 +490,13 @@ __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint3
 
   // ---- 1. stable in-warp ranks
   const typename P::Id ident = P::make(bp, s_split);
+  // Bucket of the staged key at in-tile position pos.
+  auto bucket_at = [&](uint32_t pos) -> uint32_t {
+    if constexpr (GIVEN)
+      return uint32_t(s_rb[pos]) & (B - 1);
+    else
+      return ident(s_k[pos]);
+  };
   uint32_t packed[IPT];  // (bucket << 16) | rank among same-bucket keys of this warp
   const uint32_t wbase = warp * (IPT * 32u);
   const uint32_t lt = lanemask_lt();
@@ -395,7 +511,7 @@ __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint3
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
       const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
-      const uint32_t b = GIVEN ? (uint32_t(s_rb[pos]) & (B - 1)) : ident(s_k[pos]);
+      const uint32_t b = bucket_at(pos);
       uint32_t m = FULL ? ~0u : __ballot_sync(~0u, pos < cnt);
 #pragma unroll
       for (int i = 0; i < LOGB; ++i) m &= __ballot_sync(~0u, (b >> i) & 1u) ^ xm[i];
@@ -412,7 +528,7 @@ __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint3
       for (int j = 0; j < IPT; ++j) {
         const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
         const bool valid = FULL || pos < cnt;
-        const uint32_t b = GIVEN ? (uint32_t(s_rb[pos]) & (B - 1)) : ident(s_k[pos]);
+        const uint32_t b = bucket_at(pos);
         uint32_t* e = reinterpret_cast<uint32_t*>(&wh[b * WS]);
         if (valid) atomicOr(e, 1u << lane);
         __syncwarp();
@@ -428,7 +544,7 @@ __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint3
       for (int j = 0; j < IPT; ++j) {
         const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
         const bool valid = FULL || pos < cnt;
-        const uint32_t b = GIVEN ? (uint32_t(s_rb[pos]) & (B - 1)) : ident(s_k[pos]);
+        const uint32_t b = bucket_at(pos);
 #if GMS_PEERS_MODE == 1
         uint32_t peers = __match_any_sync(~0u, b);
 #else
@@ -523,10 +639,15 @@ __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint3
         kout[s_delta[s_rb[p]] + p] = s_r[p];
       } else {
         const uint32_t src = reinterpret_cast<const uint16_t*>(s_r)[p];
-        const uint32_t key = s_k[src];
-        const uint32_t g = s_delta[L::BUCKET_BYTES ? uint32_t(s_rb[p]) : ident(key)] + p;
+        const KT key = s_k[src];
+        uint32_t b;
+        if constexpr (L::BUCKET_BYTES)
+          b = s_rb[p];
+        else
+          b = ident(key);
+        const uint32_t g = s_delta[b] + p;
         kout[g] = key;
-        vout[g] = s_v[src];
+        if constexpr (C::KV) vout[g] = s_v[src];
       }
     }
   }
@@ -535,12 +656,12 @@ __device__ __forceinline__ bool postscan_tile(uint32_t* __restrict__ kout, uint3
 
 // -------------------------------------------------------------- postscan
 // One tile of one multisplit, as the postscan sees it.
-template <class Params>
+template <class Params, class KT = uint32_t, class VT = uint32_t>
 struct TileJob {
-  const uint32_t* kin;
-  const uint32_t* vin;
-  uint32_t* kout;
-  uint32_t* vout;
+  const KT* kin;
+  const VT* vin;
+  KT* kout;
+  VT* vout;
   uint32_t n;                // keys of this multisplit
   uint32_t num_tiles;        // its tiles
   uint32_t tile;             // this tile
@@ -574,14 +695,16 @@ struct TileJob {
 // the tile's bytes are staged with its keys and the identifier is never
 // evaluated (nor prepared).
 template <class C, class P, bool PREPARE = true, bool GIVEN = false>
-__device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params>& job, ScratchHeader* hdr,
-                                             unsigned char* smem, bool* bar_live = nullptr) {
+__device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params, typename C::KT, typename C::VT>& job,
+                                             ScratchHeader* hdr, unsigned char* smem, bool* bar_live = nullptr) {
   using L = PostLayout<C, P, GIVEN>;
+  using KT = typename C::KT;
+  using VT = typename C::VT;
   constexpr uint32_t B = C::B;
   constexpr int LOGB = C::LOGB;
   constexpr uint32_t WB = C::WB;
-  uint32_t* s_k = reinterpret_cast<uint32_t*>(smem + L::OFF_K);
-  uint32_t* s_v = reinterpret_cast<uint32_t*>(smem + L::OFF_V);
+  KT* s_k = reinterpret_cast<KT*>(smem + L::OFF_K);
+  VT* s_v = reinterpret_cast<VT*>(smem + L::OFF_V);
   uint32_t* s_wh = reinterpret_cast<uint32_t*>(smem + L::OFF_WH);
   uint32_t* s_split = reinterpret_cast<uint32_t*>(smem + L::OFF_SPLIT);
   uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
@@ -589,13 +712,15 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params>& 
   const uint32_t tid = threadIdx.x;
   const uint32_t base = job.tile * C::TILE;
   const uint32_t cnt = min(C::TILE, job.n - base);
-  const uint32_t* kin = job.kin;
-  const uint32_t* vin = job.vin;
+  const KT* kin = job.kin;
+  const VT* vin = job.vin;
 
   // ---- 0. stage the tile
   uintptr_t addr_bits = reinterpret_cast<uintptr_t>(kin);
   if constexpr (C::KV) addr_bits |= reinterpret_cast<uintptr_t>(vin);
-  const uint32_t bulk = ((addr_bits & 15u) == 0) ? (cnt & ~3u) : 0u;  // elements moved by the bulk copy
+  // Elements moved by the bulk copy: a multiple of 4, so every array's part
+  // is a whole number of 16-byte pieces.
+  const uint32_t bulk = ((addr_bits & 15u) == 0) ? (cnt & ~3u) : 0u;
   if (tid == 0) *reinterpret_cast<uint32_t*>(smem + L::OFF_FLAG) = 0u;
   // Given bucket bytes: whole 16-byte pieces by the bulk copy, the rest below.
   const uint32_t bulk_b = (GIVEN && bulk != 0) ? (cnt & ~15u) : 0u;
@@ -603,17 +728,18 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params>& 
   if (tid == 0 && bulk != 0) {
     mbar_init(s_bar, 1);
     fence_mbar_init();
-    mbar_arrive_expect_tx(s_bar, (C::KV ? 2u : 1u) * bulk * 4u + bulk_b);
-    bulk_copy_g2s(s_k, kin + base, bulk * 4u, s_bar);
-    if constexpr (C::KV) bulk_copy_g2s(s_v, vin + base, bulk * 4u, s_bar);
+    mbar_arrive_expect_tx(s_bar, bulk * uint32_t(sizeof(KT) + (C::KV ? sizeof(VT) : 0)) + bulk_b);
+    bulk_copy_g2s(s_k, kin + base, bulk * uint32_t(sizeof(KT)), s_bar);
+    if constexpr (C::KV) bulk_copy_g2s(s_v, vin + base, bulk * uint32_t(sizeof(VT)), s_bar);
     if constexpr (GIVEN) {
       if (bulk_b != 0) bulk_copy_g2s(s_rb, job.bucket_bytes + base, bulk_b, s_bar);
     }
     // Pull a tile that starts about one wave of blocks later into L2, so its
     // bulk copy does not wait on DRAM (only full tiles: never past the arrays).
     if (job.prefetch_tile < job.num_tiles - 1u) {
-      bulk_prefetch_l2(kin + size_t(job.prefetch_tile) * C::TILE, C::TILE * 4u);
-      if constexpr (C::KV) bulk_prefetch_l2(vin + size_t(job.prefetch_tile) * C::TILE, C::TILE * 4u);
+      bulk_prefetch_l2(kin + size_t(job.prefetch_tile) * C::TILE, C::TILE * uint32_t(sizeof(KT)));
+      if constexpr (C::KV)
+        bulk_prefetch_l2(vin + size_t(job.prefetch_tile) * C::TILE, C::TILE * uint32_t(sizeof(VT)));
     }
   }
   for (uint32_t i = bulk + tid; i < cnt; i += C::THREADS) {
@@ -660,7 +786,8 @@ __device__ __forceinline__ void postscan_run(uint32_t first, uint32_t last, uint
   uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
   uint32_t prepared_for = ~0u;  // owner whose parameters the shared area holds
   for (uint32_t t = first; t < last; t += stride) {
-    const TileJob<typename P::Params> job = job_at(t, last - t > stride ? t + stride : ~0u);
+    const TileJob<typename P::Params, typename C::KT, typename C::VT> job =
+        job_at(t, last - t > stride ? t + stride : ~0u);
     if (job.owner != prepared_for) {  // block-uniform: every thread reads the same job
       P::prepare(s_split, job.bp);
       prepared_for = job.owner;
@@ -677,11 +804,11 @@ __device__ __forceinline__ void postscan_run(uint32_t first, uint32_t last, uint
 // come from bucket_bytes (written by the prescan).
 template <class C, class P, bool GIVEN = false>
 __global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P, GIVEN>::MIN_BLOCKS)) postscan_kernel(
-    const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
-    uint32_t* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
+    const typename C::KT* __restrict__ kin, const typename C::VT* __restrict__ vin, typename C::KT* __restrict__ kout,
+    typename C::VT* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
     typename P::Params bp, ScratchHeader* hdr, uint32_t prefetch_dist, const uint8_t* __restrict__ bucket_bytes) {
   extern __shared__ __align__(128) unsigned char smem[];
-  const TileJob<typename P::Params> job{kin,        vin,     kout, vout,
+  const TileJob<typename P::Params, typename C::KT, typename C::VT> job{kin,        vin,     kout, vout,
                                         n,          num_tiles, blockIdx.x, offsets,
                                         0u,         prefetch_dist != 0 ? blockIdx.x + prefetch_dist : ~0u,
                                         bp,         0u,      bucket_bytes};
@@ -694,14 +821,15 @@ __global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P, GIVEN>::MIN_BLOC
 // so partly written sectors merge in L2 before they reach DRAM.
 template <class C, class P>
 __global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P>::MIN_BLOCKS)) postscan_persistent_kernel(
-    const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
-    uint32_t* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
+    const typename C::KT* __restrict__ kin, const typename C::VT* __restrict__ vin, typename C::KT* __restrict__ kout,
+    typename C::VT* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
     typename P::Params bp, ScratchHeader* hdr) {
   extern __shared__ __align__(128) unsigned char smem[];
   postscan_run<C, P>(
       blockIdx.x, num_tiles, gridDim.x,
       [&](uint32_t t, uint32_t prefetch) {
-        return TileJob<typename P::Params>{kin, vin, kout, vout, n, num_tiles, t, offsets, 0u, prefetch, bp, 0u};
+        return TileJob<typename P::Params, typename C::KT, typename C::VT>{
+            kin, vin, kout, vout, n, num_tiles, t, offsets, 0u, prefetch, bp, 0u};
       },
       hdr, smem);
 }

@@ -7,6 +7,7 @@ pseudorandom number generators", OOPSLA 2014), so element i depends only on
 
 Distributions (one per benchmark configuration):
   uniform_u32   keys uniform over [0, 2^32)
+  uniform_u64   keys uniform over [0, 2^64) (64-bit keys)
   and4_u32      AND of 4 uniform draws (each bit set with p = 1/16)
   zipf_u32      Zipf(s) over `distinct` key values drawn uniformly over [0, 2^32)
   range_splitters  B sorted splitters, splitter[0] = 0, the rest uniform
@@ -60,6 +61,25 @@ def uniform_u32(n: int, seed: int, device="cpu") -> torch.Tensor:
         c = min(CHUNK, n - s)
         out[s:s + c] = _hi32(splitmix64(seed, s, c, device))
     return out
+
+
+def uniform_u64(n: int, seed: int, device="cpu") -> torch.Tensor:
+    """n keys uniform over [0, 2^64): the full splitmix64 output, as an int64
+    tensor of uint64 bit patterns."""
+    out = torch.empty(n, dtype=torch.int64, device=device)
+    for s in range(0, n, CHUNK):
+        c = min(CHUNK, n - s)
+        out[s:s + c] = splitmix64(seed, s, c, device)
+    return out
+
+
+def as_u64(t: torch.Tensor) -> np.ndarray:
+    """Host numpy uint64 view of an int64 tensor."""
+    return t.detach().cpu().numpy().view(np.uint64)
+
+
+def from_u64(a: np.ndarray, device="cpu") -> torch.Tensor:
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint64).view(np.int64)).to(device)
 
 
 def and4_u32(n: int, seed: int, device="cpu") -> torch.Tensor:

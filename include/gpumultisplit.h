@@ -199,6 +199,48 @@ gms_status gms_sort_bits_key_value(const uint32_t* d_key_in, uint32_t* d_key_out
                                    uint32_t* d_value_out, uint32_t n, int begin_bit, int end_bit, int digit_bits,
                                    void* d_scratch, size_t scratch_bytes, gms_stream_t stream);
 
+/* ------------------------------------------- 64-bit keys and values */
+/* No counterpart in the reference, whose kernels hold 32-bit keys and values
+ * (src/kernels/bms/bms_postscan.cuh:38).  Keys are 4 or 8 bytes (key_bytes),
+ * values 0 (key-only), 4 or 8 bytes (value_bytes); each array is aligned to
+ * its element size.  The identifier kinds are those of gms_bucket_desc, on
+ * the key's full width:
+ *   DELTA       key * B >> 64 for 8-byte keys (>> 32 for 4-byte keys)
+ *   DIV         (key / param) mod B
+ *   BITS        (key >> shift) & (B-1), shift < 64
+ *   RANGE       upper_bound(d_splitters[0..B), key) - 1, -1 read as B-1; the
+ *               splitters are keys of key_bytes each
+ *   MASK        (key & param) != 0
+ *   EVEN_FLOAT  (uint32)((float)(key - lower) * inverse_delta) mod B, with the
+ *               same round-to-nearest conversions and truncation as for 4-byte keys
+ * With 4-byte keys param and lower must fit in 32 bits.  Output order, offsets
+ * and stability are those of gms_multisplit_key_value.  8-byte keys are
+ * identified once, in the first pass, and keep their buckets as one byte per
+ * key in the scratch, so their scratch is always the size
+ * gms_multisplit_wide_scratch_bytes reports. */
+typedef struct gms_bucket_desc64 {
+  int32_t kind;                /* gms_bucket_kind */
+  uint32_t num_buckets;        /* B: 2..256 (a power of two for BITS) */
+  uint32_t shift;              /* BITS */
+  float inverse_delta;         /* EVEN_FLOAT: 1 / bin width */
+  uint64_t param;              /* DIV: divisor (non-zero); MASK: mask */
+  uint64_t lower;              /* EVEN_FLOAT: lower level */
+  const void* d_splitters;     /* RANGE: B sorted splitters of key_bytes each, device memory */
+} gms_bucket_desc64;
+
+gms_status gms_multisplit_wide_scratch_bytes(uint32_t max_elements, uint32_t num_buckets, int key_bytes,
+                                             int value_bytes, size_t* bytes);
+gms_status gms_multisplit_wide(const void* d_key_in, const void* d_value_in, void* d_key_out, void* d_value_out,
+                               uint32_t n, int key_bytes, int value_bytes, const gms_bucket_desc64* desc,
+                               void* d_scratch, size_t scratch_bytes, uint32_t* h_offsets, gms_stream_t stream);
+/* Stable sort by key bits [begin_bit, end_bit), end_bit <= 8 * key_bytes, in
+ * digits of digit_bits (4..8) bits, least significant first. */
+gms_status gms_sort_wide_scratch_bytes(uint32_t max_elements, int key_bytes, int value_bytes, int begin_bit,
+                                       int end_bit, int digit_bits, size_t* bytes);
+gms_status gms_sort_wide(const void* d_key_in, void* d_key_out, const void* d_value_in, void* d_value_out, uint32_t n,
+                         int key_bytes, int value_bytes, int begin_bit, int end_bit, int digit_bits, void* d_scratch,
+                         size_t scratch_bytes, gms_stream_t stream);
+
 /* ----------------------------------------------------------- compaction */
 /* Replaces compaction_allocate_key_only / _key_value
  * (src/kernels/compaction/multisplit2_compaction.cuh:491-517). */

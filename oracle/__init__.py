@@ -7,7 +7,8 @@ calls it.
   liboracle.so   plain-C restatement of the reference's CPU multisplit
                  (src/cpu_functions.h:155-288) plus histogram, tile counts,
                  the sort digit schedules, partial-key sorts and compaction
-                 (oracle.c cites each).
+                 (oracle.c cites each), and the same multisplit and sort
+                 for 64-bit keys.
   libgms_ref.so  the reference's OWN cpu_multisplit_general /
                  cpu_multisplit_pairs_general compiled from its sources
                  (ref_shim.cpp, `make ref`); built only where the reference
@@ -208,6 +209,87 @@ def uniform_u32(n: int, seed: int) -> np.ndarray:
     out = np.empty(n, np.uint32)
     lib().oracle_uniform_u32(_p(out), ctypes.c_uint64(n), ctypes.c_uint64(seed))
     return out
+
+
+# ------------------------------------------------------------- 64-bit keys
+
+
+class _CDesc64(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("num_buckets", ctypes.c_uint32), ("shift", ctypes.c_uint32),
+                ("inverse_delta", ctypes.c_float), ("param", ctypes.c_uint64), ("lower", ctypes.c_uint64),
+                ("splitters", ctypes.c_void_p)]
+
+
+@dataclass
+class Desc64:
+    """Bucket identifier on 64-bit keys (same meaning as gms_bucket_desc64; splitters on the host)."""
+
+    kind: int
+    num_buckets: int
+    shift: int = 0
+    param: int = 0
+    lower: int = 0
+    inverse_delta: float = 0.0
+    splitters: np.ndarray | None = field(default=None, repr=False)
+
+    def c(self) -> _CDesc64:
+        d = _CDesc64(self.kind, self.num_buckets, self.shift, self.inverse_delta, self.param, self.lower, None)
+        if self.splitters is not None:
+            self._keep = np.ascontiguousarray(self.splitters, dtype=np.uint64)
+            d.splitters = self._keep.ctypes.data
+        return d
+
+
+def _u64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint64)
+
+
+def _values(values):
+    """(contiguous array, element bytes) of a value array of 4- or 8-byte elements, or (None, 0)."""
+    if values is None:
+        return None, 0
+    v = np.ascontiguousarray(values)
+    if v.dtype.itemsize not in (4, 8):
+        raise ValueError("values must have 4- or 8-byte elements")
+    return v, v.dtype.itemsize
+
+
+def buckets64(keys, d: Desc64) -> np.ndarray:
+    keys = _u64(keys)
+    cd = d.c()
+    f = lib().oracle_bucket64
+    f.restype = ctypes.c_uint32
+    return np.array([f(ctypes.byref(cd), ctypes.c_uint64(int(k))) for k in keys], dtype=np.uint32)
+
+
+def multisplit64(keys, d: Desc64, values=None):
+    """Stable multisplit of 64-bit keys -> (keys_out, values_out or None, bucket offsets).
+    Values are any 4- or 8-byte elements."""
+    keys = _u64(keys)
+    n = keys.size
+    v, vb = _values(values)
+    kout = np.empty(n, np.uint64)
+    vout = np.empty_like(v) if v is not None else None
+    offs = np.empty(d.num_buckets, np.uint32)
+    cd = d.c()
+    lib().oracle_multisplit64(_p(keys), _p(kout), _p(v), _p(vout), ctypes.c_int(vb), ctypes.c_uint32(n),
+                              ctypes.byref(cd), _p(offs))
+    return kout, vout, offs
+
+
+def sort_bits64(keys, values=None, begin_bit: int = 0, end_bit: int = 64, digit_bits: int = 8):
+    """Stable sort of 64-bit keys by bits [begin_bit, end_bit) in digit_bits-wide passes."""
+    keys = _u64(keys)
+    n = keys.size
+    v, vb = _values(values)
+    kout, tk = np.empty(n, np.uint64), np.empty(n, np.uint64)
+    vout = np.empty_like(v) if v is not None else None
+    tv = np.empty_like(v) if v is not None else None
+    rc = lib().oracle_sort_bits64(_p(keys), _p(kout), _p(v), _p(vout), ctypes.c_int(vb), ctypes.c_uint32(n), _p(tk),
+                                  _p(tv), ctypes.c_int(begin_bit), ctypes.c_int(end_bit), ctypes.c_int(digit_bits))
+    if rc != 0:
+        raise ValueError("invalid bit range or digit width")
+    return kout, vout
 
 
 # ------------------------------------------------ the reference's own CPU code

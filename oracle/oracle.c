@@ -283,3 +283,107 @@ void oracle_uniform_u32(uint32_t* out, uint64_t n, uint64_t seed) {
     out[i] = (uint32_t)(z >> 32);
   }
 }
+
+/* ---------------------------------------------------------------------
+ * 64-bit keys.  The reference's multisplit holds 32-bit keys only
+ * (src/kernels/bms/bms_postscan.cuh:38); this restates its CPU algorithm
+ * (histogram -> exclusive scan -> stable placement, src/cpu_functions.h:155-288)
+ * for 64-bit keys, with every identifier kind on the key's full width.
+ * Values are moved as opaque elements of value_bytes (0 = key-only, 4 or 8).
+ */
+uint32_t oracle_bucket64(const oracle_desc64* d, uint64_t key) {
+  const uint32_t B = d->num_buckets;
+  switch (d->kind) {
+    case ORACLE_DELTA: {
+      /* key * B >> 64: the high word of the 128-bit product, from 32-bit halves. */
+      const uint64_t lo = (key & 0xFFFFFFFFull) * B, hi = (key >> 32) * B;
+      return (uint32_t)((hi + (lo >> 32)) >> 32);
+    }
+    case ORACLE_DIV:
+      return (uint32_t)((key / d->param) % B);
+    case ORACLE_BITS:
+      return (uint32_t)((d->shift >= 64u ? 0u : (key >> d->shift)) % B);
+    case ORACLE_RANGE: {
+      uint32_t lo = 0, hi = B;
+      while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2u;
+        if (d->splitters[mid] <= key)
+          lo = mid + 1u;
+        else
+          hi = mid;
+      }
+      return lo == 0u ? B - 1u : lo - 1u;
+    }
+    case ORACLE_MASK:
+      return (key & d->param) ? 1u : 0u;
+    case ORACLE_EVEN_FLOAT: {
+      /* uint64 -> float (round to nearest even, as __ull2float_rn), float
+       * multiply, saturating truncation: as for 32-bit keys. */
+      const float x = (float)(uint64_t)(key - d->lower) * d->inverse_delta;
+      uint32_t b;
+      if (!(x > 0.0f))
+        b = 0u;
+      else if (x >= 4294967296.0f)
+        b = 0xFFFFFFFFu;
+      else
+        b = (uint32_t)x;
+      return b % B;
+    }
+    default:
+      return 0u;
+  }
+}
+
+void oracle_multisplit64(const uint64_t* kin, uint64_t* kout, const void* vin, void* vout, int value_bytes,
+                         uint32_t n, const oracle_desc64* d, uint32_t* offsets) {
+  const uint32_t B = d->num_buckets;
+  uint32_t* bins = (uint32_t*)calloc(B, sizeof(uint32_t));
+  uint32_t* next = (uint32_t*)calloc(B, sizeof(uint32_t));
+  for (uint32_t i = 0; i < n; ++i) bins[oracle_bucket64(d, kin[i])]++;
+  uint32_t run = 0;
+  for (uint32_t b = 0; b < B; ++b) {
+    next[b] = run;
+    run += bins[b];
+  }
+  if (offsets) memcpy(offsets, next, B * sizeof(uint32_t));
+  const size_t vb = (size_t)value_bytes;
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t dst = next[oracle_bucket64(d, kin[i])]++;
+    kout[dst] = kin[i];
+    if (vb) memcpy((char*)vout + (size_t)dst * vb, (const char*)vin + (size_t)i * vb, vb);
+  }
+  free(bins);
+  free(next);
+}
+
+/* Stable sort of 64-bit keys by bits [begin_bit, end_bit), end_bit <= 64, in
+ * digits of digit_bits bits, least significant first (the last one narrower).
+ * tmp_k / tmp_v hold n elements.  Returns 0, or -1 for an invalid range. */
+int oracle_sort_bits64(const uint64_t* kin, uint64_t* kout, const void* vin, void* vout, int value_bytes, uint32_t n,
+                       uint64_t* tmp_k, void* tmp_v, int begin_bit, int end_bit, int digit_bits) {
+  if (digit_bits < 4 || digit_bits > 8 || begin_bit < 0 || end_bit > 64 || begin_bit > end_bit) return -1;
+  const int P = (end_bit - begin_bit + digit_bits - 1) / digit_bits;
+  if (P == 0) {
+    memcpy(kout, kin, sizeof(uint64_t) * n);
+    if (value_bytes) memcpy(vout, vin, (size_t)value_bytes * n);
+    return 0;
+  }
+  const uint64_t* src_k = kin;
+  const void* src_v = vin;
+  for (int p = 0; p < P; ++p) {
+    const int shift = begin_bit + p * digit_bits;
+    const int w = end_bit - shift < digit_bits ? end_bit - shift : digit_bits;
+    const int to_out = ((P - 1 - p) % 2) == 0;
+    uint64_t* dk = to_out ? kout : tmp_k;
+    void* dv = to_out ? vout : tmp_v;
+    oracle_desc64 d;
+    memset(&d, 0, sizeof(d));
+    d.kind = ORACLE_BITS;
+    d.num_buckets = 1u << w;
+    d.shift = (uint32_t)shift;
+    oracle_multisplit64(src_k, dk, src_v, dv, value_bytes, n, &d, NULL);
+    src_k = dk;
+    src_v = dv;
+  }
+  return 0;
+}

@@ -47,6 +47,23 @@ void oracle_multisplit_mt(const uint32_t* kin, uint32_t* kout, const uint32_t* v
                           const oracle_desc* d, int threads);
 void oracle_uniform_u32(uint32_t* out, uint64_t n, uint64_t seed);
 
+/* 64-bit keys; same field order as gms_bucket_desc64 (splitters on the host). */
+typedef struct oracle_desc64 {
+  int32_t kind;
+  uint32_t num_buckets;
+  uint32_t shift;
+  float inverse_delta;
+  uint64_t param;
+  uint64_t lower;
+  const uint64_t* splitters;
+} oracle_desc64;
+
+uint32_t oracle_bucket64(const oracle_desc64* d, uint64_t key);
+void oracle_multisplit64(const uint64_t* kin, uint64_t* kout, const void* vin, void* vout, int value_bytes,
+                         uint32_t n, const oracle_desc64* d, uint32_t* offsets);
+int oracle_sort_bits64(const uint64_t* kin, uint64_t* kout, const void* vin, void* vout, int value_bytes, uint32_t n,
+                       uint64_t* tmp_k, void* tmp_v, int begin_bit, int end_bit, int digit_bits);
+
 #ifdef __cplusplus
 }
 #endif

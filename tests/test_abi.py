@@ -112,6 +112,84 @@ def test_argument_checks_before_cuda(gms_lib):
                                            None) == _lib.GMS_ERROR_INVALID_VALUE
 
 
+def test_wide_argument_checks_before_cuda(gms_lib):
+    """64-bit entry points: calls that fail on their arguments, before any CUDA work."""
+    f = gms_lib.gms_multisplit_wide
+    k_in, k_out, v_in, v_out, scr = 1 << 20, 1 << 24, 1 << 28, 1 << 30, 1 << 32
+    d = _lib.BucketDesc64(kind=_lib.GMS_BUCKET_DELTA, num_buckets=256)
+    ok = ctypes.c_size_t()
+    assert gms_lib.gms_multisplit_wide_scratch_bytes(1000, 256, 8, 8, ctypes.byref(ok)) == 0
+    big = 1 << 26
+    for kb, vb in ((3, 0), (8, 2), (16, 8), (8, 12)):  # widths other than 4/8 (keys) and 0/4/8 (values)
+        assert f(k_in, v_in, k_out, v_out, 1000, kb, vb, ctypes.byref(d), scr, big, None, None) == \
+            _lib.GMS_ERROR_INVALID_VALUE
+        assert gms_lib.gms_multisplit_wide_scratch_bytes(1000, 256, kb, vb, ctypes.byref(ok)) == \
+            _lib.GMS_ERROR_INVALID_VALUE
+    bad = [
+        (_lib.BucketDesc64(kind=_lib.GMS_BUCKET_DELTA, num_buckets=300), _lib.GMS_ERROR_UNSUPPORTED_BUCKETS),
+        (_lib.BucketDesc64(kind=_lib.GMS_BUCKET_BITS, num_buckets=12), _lib.GMS_ERROR_UNSUPPORTED_BUCKETS),
+        (_lib.BucketDesc64(kind=_lib.GMS_BUCKET_BITS, num_buckets=16, shift=64), _lib.GMS_ERROR_INVALID_VALUE),
+        (_lib.BucketDesc64(kind=_lib.GMS_BUCKET_DIV, num_buckets=16, param=0), _lib.GMS_ERROR_INVALID_VALUE),
+        (_lib.BucketDesc64(kind=_lib.GMS_BUCKET_RANGE, num_buckets=16), _lib.GMS_ERROR_INVALID_VALUE),
+        (_lib.BucketDesc64(kind=42, num_buckets=16), _lib.GMS_ERROR_INVALID_VALUE),
+    ]
+    for bd, want in bad:
+        assert f(k_in, v_in, k_out, v_out, 1000, 8, 8, ctypes.byref(bd), scr, big, None, None) == want
+    # 32-bit keys: 64-bit parameters must fit in 32 bits
+    wide_param = _lib.BucketDesc64(kind=_lib.GMS_BUCKET_MASK, num_buckets=2, param=1 << 40)
+    assert f(k_in, v_in, k_out, v_out, 1000, 4, 8, ctypes.byref(wide_param), scr, big, None, None) == \
+        _lib.GMS_ERROR_INVALID_VALUE
+    # keys not aligned to their 8 bytes, values not aligned to theirs
+    assert f(k_in + 4, v_in, k_out, v_out, 1000, 8, 8, ctypes.byref(d), scr, big, None, None) == \
+        _lib.GMS_ERROR_INVALID_VALUE
+    assert f(k_in, v_in + 4, k_out, v_out, 1000, 8, 8, ctypes.byref(d), scr, big, None, None) == \
+        _lib.GMS_ERROR_INVALID_VALUE
+    # outputs overlapping (8-byte elements: 8 bytes apart overlap)
+    assert f(k_in, v_in, k_out, k_out + 8, 1000, 8, 8, ctypes.byref(d), scr, big, None, None) == \
+        _lib.GMS_ERROR_INVALID_VALUE
+    # 64-bit keys need the bucket bytes: the reported size, not less
+    need = ctypes.c_size_t()
+    assert gms_lib.gms_multisplit_wide_scratch_bytes(100000, 256, 8, 8, ctypes.byref(need)) == 0
+    assert f(k_in, v_in, k_out, v_out, 100000, 8, 8, ctypes.byref(d), scr, need.value - 256, None, None) == \
+        _lib.GMS_ERROR_SCRATCH_TOO_SMALL
+    # sorts: bit ranges beyond the key width
+    s = gms_lib.gms_sort_wide_scratch_bytes
+    assert s(1000, 8, 8, 0, 64, 8, ctypes.byref(ok)) == 0
+    assert s(1000, 8, 8, 0, 65, 8, ctypes.byref(ok)) == _lib.GMS_ERROR_INVALID_VALUE
+    assert s(1000, 4, 8, 0, 33, 8, ctypes.byref(ok)) == _lib.GMS_ERROR_INVALID_VALUE
+    assert s(1000, 8, 0, 0, 64, 9, ctypes.byref(ok)) == _lib.GMS_ERROR_INVALID_VALUE
+    # n = 0 is a no-op that succeeds
+    assert f(None, None, None, None, 0, 8, 8, ctypes.byref(d), None, 0, None, None) == 0
+
+
+def test_wide_scratch_sizes(gms_lib):
+    """64-bit elements: tiles of 2048 keys above 8 bytes per key, bucket bytes
+    always counted; a sort adds its ping-pong keys and values."""
+    def nbytes(n, B, kb, vb):
+        out = ctypes.c_size_t()
+        assert gms_lib.gms_multisplit_wide_scratch_bytes(n, B, kb, vb, ctypes.byref(out)) == 0
+        return out.value
+
+    def align(x):
+        return (x + 255) // 256 * 256
+
+    n = 1 << 20
+    # 32-bit keys and values: the same as gms_multisplit_scratch_bytes
+    for kv in (0, 1):
+        ref = ctypes.c_size_t()
+        assert gms_lib.gms_multisplit_scratch_bytes(n, 256, kv, ctypes.byref(ref)) == 0
+        assert nbytes(n, 256, 4, 4 * kv) == ref.value
+    for kb, vb, tile in ((8, 0, 4096), (4, 8, 2048), (8, 4, 2048), (8, 8, 2048)):
+        tiles = (n + tile - 1) // tile
+        m = 256 * tiles
+        chunks = (m + 4095) // 4096
+        expect = align(align(align(256 + 4 * m) + 8 * chunks) + n)
+        assert nbytes(n, 256, kb, vb) == expect, (kb, vb)
+    srt = ctypes.c_size_t()
+    assert gms_lib.gms_sort_wide_scratch_bytes(n, 8, 8, 0, 64, 8, ctypes.byref(srt)) == 0
+    assert srt.value == align(align(nbytes(n, 256, 8, 8)) + 8 * n) + 8 * n
+
+
 def test_sort_scratch_covers_both_digit_widths(gms_lib):
     for n in (1, 1000, 1 << 20):
         for kv in (0, 1):

@@ -175,3 +175,37 @@ def test_oracle_buckets_any_count(oracle_mod):
             ko, vo, _ = o.multisplit(keys, d, vals)
             rk, rv = o.ref_multisplit(keys, d, vals)
             assert np.array_equal(ko, rk) and np.array_equal(vo, rv)
+
+
+def test_oracle_64bit_keys_against_numpy(oracle_mod):
+    """The 64-bit restatement equals an independent one: numpy's stable argsort
+    of the bucket ids (multisplit) and of the key bits (sort)."""
+    o = oracle_mod
+    keys = datagen.as_u64(datagen.uniform_u64(6000, 17))
+    keys[:4] = [0, 2**64 - 1, 2**63, 2**32 - 1]
+    vals = np.arange(keys.size, dtype=np.uint64) * np.uint64(3)
+    for B in (2, 3, 100, 256):
+        k = [int(x) for x in keys]
+        spl = np.concatenate([[0], np.sort(datagen.as_u64(datagen.uniform_u64(B - 1, B)))]).astype(np.uint64)
+        ub = np.searchsorted(spl, keys, side="right").astype(np.int64) - 1
+        cases = [
+            (o.Desc64(o.DELTA, B), np.array([(x * B) >> 64 for x in k])),
+            (o.Desc64(o.DIV, B, param=(1 << 60) + 12345), np.array([(x // ((1 << 60) + 12345)) % B for x in k])),
+            (o.Desc64(o.RANGE, B, splitters=spl), np.where(ub < 0, B - 1, ub)),
+            (o.Desc64(o.MASK, B, param=1 << 45), np.array([1 if x & (1 << 45) else 0 for x in k])),
+        ]
+        if B & (B - 1) == 0:
+            cases.append((o.Desc64(o.BITS, B, shift=40), np.array([(x >> 40) % B for x in k])))
+        for d, ids in cases:
+            assert np.array_equal(o.buckets64(keys, d), ids.astype(np.uint32))
+            ko, vo, offs = o.multisplit64(keys, d, vals)
+            order = np.argsort(ids, kind="stable")
+            assert np.array_equal(ko, keys[order]) and np.array_equal(vo, vals[order])
+            assert np.array_equal(offs, np.searchsorted(np.sort(ids), np.arange(B)).astype(np.uint32))
+        f = o.buckets64(keys, o.Desc64(o.EVEN_FLOAT, B, lower=2**40, inverse_delta=B / 2**64))
+        assert f.max() < B
+    ks, vs = o.sort_bits64(keys, vals, 0, 64, 8)
+    assert np.array_equal(ks, np.sort(keys)) and np.array_equal(vs, vals[np.argsort(keys, kind="stable")])
+    ks, vs = o.sort_bits64(keys, vals.astype(np.uint32), 13, 47, 7)
+    sub = (keys >> np.uint64(13)) & np.uint64((1 << 34) - 1)
+    assert np.array_equal(vs, vals.astype(np.uint32)[np.argsort(sub, kind="stable")])
