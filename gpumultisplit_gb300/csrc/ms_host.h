@@ -17,10 +17,30 @@ namespace gms {
 // every B (16 x 8 and 16 x 16 shapes, and 8 x 8, were slower); at B = 256 the
 // count matrix is then 1 byte per key.
 //
-// With 64-bit keys or values (KW / VW = 32-bit words per key / value) a tile
-// of more than 8 bytes per key is halved to 2048 keys, so that the staged
-// tile still leaves room for five or six blocks per SM.
-constexpr int tile_ipt(bool kv, int kw, int vw) { return 4 * kw + (kv ? 4 * vw : 0) <= 8 ? 16 : 8; }
+// With 64-bit keys or values (KW / VW = 32-bit words per key / value) the
+// keys per thread (a multiple of 4) depend on the bytes a key brings, e:
+//   e = 8, 64-bit keys alone  GMS_WIDE8_IPT (16)
+//   e = 12                    GMS_WIDE12_IPT (16)
+//   e = 16                    GMS_WIDE16_IPT (12: 3072-key tiles of 62 KB staged,
+//                             three blocks per SM)
+// Measured at 2^28 keys, B = 256: 64-bit keys with 64-bit values ran at 104 /
+// 122 / 116 Gkeys/s with 8 / 12 / 16 keys per thread, the 12-byte pairs at
+// 110-123 / 131-153 / 142-167.
+#ifndef GMS_WIDE8_IPT
+#define GMS_WIDE8_IPT 16
+#endif
+#ifndef GMS_WIDE12_IPT
+#define GMS_WIDE12_IPT 16
+#endif
+#ifndef GMS_WIDE16_IPT
+#define GMS_WIDE16_IPT 12
+#endif
+constexpr int tile_ipt(bool kv, int kw, int vw) {
+  return kw == 1 && (!kv || vw == 1) ? 16
+         : 4 * kw + (kv ? 4 * vw : 0) <= 8 ? GMS_WIDE8_IPT
+         : 4 * kw + (kv ? 4 * vw : 0) <= 12 ? GMS_WIDE12_IPT
+                                            : GMS_WIDE16_IPT;
+}
 
 template <int LOGB, bool KV, int KW = 1, int VW = 1>
 struct TileShape {

@@ -163,8 +163,8 @@ def test_wide_argument_checks_before_cuda(gms_lib):
 
 
 def test_wide_scratch_sizes(gms_lib):
-    """64-bit elements: tiles of 2048 keys above 8 bytes per key, bucket bytes
-    always counted; a sort adds its ping-pong keys and values."""
+    """64-bit elements: 4096-key tiles up to 12 bytes per key, 3072 at 16,
+    bucket bytes always counted; a sort adds its ping-pong keys and values."""
     def nbytes(n, B, kb, vb):
         out = ctypes.c_size_t()
         assert gms_lib.gms_multisplit_wide_scratch_bytes(n, B, kb, vb, ctypes.byref(out)) == 0
@@ -179,7 +179,7 @@ def test_wide_scratch_sizes(gms_lib):
         ref = ctypes.c_size_t()
         assert gms_lib.gms_multisplit_scratch_bytes(n, 256, kv, ctypes.byref(ref)) == 0
         assert nbytes(n, 256, 4, 4 * kv) == ref.value
-    for kb, vb, tile in ((8, 0, 4096), (4, 8, 2048), (8, 4, 2048), (8, 8, 2048)):
+    for kb, vb, tile in ((8, 0, 4096), (4, 8, 4096), (8, 4, 4096), (8, 8, 3072)):
         tiles = (n + tile - 1) // tile
         m = 256 * tiles
         chunks = (m + 4095) // 4096
