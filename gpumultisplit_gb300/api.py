@@ -209,7 +209,7 @@ class multisplit_context:
         """Bucket-major count matrix inside the scratch, laid out for num_elements =
         the allocated capacity (after a call: global offsets, offset(b, tile) at
         [b * num_sub_prob + tile]).  It always starts 256 bytes into the scratch."""
-        if self.d_temp_storage is None:
+        if self.d_temp_storage is None or self.num_buckets > 256:
             return None
         import torch
 
@@ -225,8 +225,9 @@ def _ms_allocate(num_elements: int, context: multisplit_context, key_value: bool
     check(lib.gms_multisplit_scratch_bytes(num_elements, context.num_buckets, int(key_value), ctypes.byref(nbytes)),
           "multisplit_allocate")
     tile, tiles = ctypes.c_uint32(), ctypes.c_uint32()
-    check(lib.gms_multisplit_geometry(num_elements, context.num_buckets, int(key_value), ctypes.byref(tile),
-                                      ctypes.byref(tiles), None), "multisplit_geometry")
+    if context.num_buckets <= 256:  # above 256 buckets there are two digit passes and no single count matrix
+        check(lib.gms_multisplit_geometry(num_elements, context.num_buckets, int(key_value), ctypes.byref(tile),
+                                          ctypes.byref(tiles), None), "multisplit_geometry")
     context.size_sub_prob = tile.value
     context.num_sub_prob = tiles.value
     context.num_blocks = tiles.value

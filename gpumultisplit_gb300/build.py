@@ -35,11 +35,12 @@ def nvcc_path() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build gpumultisplit_gb300")
 
 
-# inst_batch.cu is compiled once per (identifier kind, tile variant) and
-# inst_wide.cu once per identifier kind; the counts match NUM_KINDS in
+# inst_batch.cu is compiled once per (identifier kind, tile variant),
+# inst_wide.cu and inst_big.cu once per identifier kind; the counts match NUM_KINDS in
 # gms_device.cuh and kNumTileVariants in ms_host.h.
 BATCH_INST = "inst_batch.cu"
 WIDE_INST = "inst_wide.cu"
+BIG_INST = "inst_big.cu"
 NUM_KINDS = 6
 NUM_TILE_VARIANTS = 4
 
@@ -56,7 +57,7 @@ def _units() -> list[tuple[Path, str, list[str]]]:
             for k in range(NUM_KINDS):
                 for v in range(NUM_TILE_VARIANTS):
                     units.append((s, f"{s.stem}_k{k}_v{v}", [f"-DGMS_INST_KIND={k}", f"-DGMS_INST_VARIANT={v}"]))
-        elif s.name == WIDE_INST:
+        elif s.name in (WIDE_INST, BIG_INST):
             for k in range(NUM_KINDS):
                 units.append((s, f"{s.stem}_k{k}", [f"-DGMS_INST_KIND={k}"]))
         else:

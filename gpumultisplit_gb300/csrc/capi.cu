@@ -270,6 +270,139 @@ gms_status compaction_impl(const uint32_t* kin, const uint32_t* vin, uint32_t* k
   return cuda_status(e);
 }
 
+// ------------------------------------------------ more than 256 buckets
+// B in (256, 65536] (RANGE: to GMS_RANGE_BIG_MAX splitters), 32-bit keys and
+// values, through the one-call entry points: two stable multisplits on the
+// digits of the bucket id, id & 255 into the scratch's ping-pong buffers, then
+// id >> 8 into the output.  Offsets come from a histogram of the whole ids.
+int big_high_logb(uint32_t B) {
+  const uint32_t hi = (B + 255u) / 256u;  // values of the high digit
+  int l = 1;
+  while ((1u << l) < hi) ++l;
+  return l;
+}
+
+struct BigLayout {
+  int logb_hi;
+  size_t ms_bytes;  // scratch of either pass (with its bucket bytes)
+  size_t off_keys, off_vals, off_hist, bytes;
+};
+
+BigLayout big_layout(uint32_t n, uint32_t B, bool kv) {
+  BigLayout L;
+  L.logb_hi = big_high_logb(B);
+  const size_t a = make_geometry(n, 8, kv).bytes_full, b = make_geometry(n, L.logb_hi, kv).bytes_full;
+  L.ms_bytes = a > b ? a : b;
+  L.off_keys = align_up(L.ms_bytes, 256);
+  L.off_vals = align_up(L.off_keys + size_t(n) * 4, 256);
+  L.off_hist = kv ? align_up(L.off_vals + size_t(n) * 4, 256) : L.off_vals;
+  L.bytes = align_up(L.off_hist + size_t(B) * 4, 256);
+  return L;
+}
+
+bool is_big(const gms_bucket_desc* d) { return d != nullptr && d->num_buckets > 256; }
+
+gms_status check_big_desc(const gms_bucket_desc* d) {
+  if (d == nullptr) return GMS_ERROR_INVALID_VALUE;
+  const uint32_t B = d->num_buckets;
+  if (B <= 256 || B > BIG_MAX_BUCKETS) return GMS_ERROR_UNSUPPORTED_BUCKETS;
+  switch (d->kind) {
+    case GMS_BUCKET_BITS:
+      return (B & (B - 1)) == 0 ? GMS_SUCCESS : GMS_ERROR_UNSUPPORTED_BUCKETS;
+    case GMS_BUCKET_DELTA:
+    case GMS_BUCKET_MASK:
+    case GMS_BUCKET_EVEN_FLOAT:
+      return GMS_SUCCESS;
+    case GMS_BUCKET_DIV:
+      return d->param != 0 ? GMS_SUCCESS : GMS_ERROR_INVALID_VALUE;
+    case GMS_BUCKET_RANGE:
+      if (B > GMS_RANGE_BIG_MAX) return GMS_ERROR_UNSUPPORTED_BUCKETS;
+      return d->d_splitters != nullptr ? GMS_SUCCESS : GMS_ERROR_INVALID_VALUE;
+    default:
+      return GMS_ERROR_INVALID_VALUE;
+  }
+}
+
+cudaError_t dispatch_digit_prescan(int kind, const DigitPass& c) {
+  switch (kind) {
+    case KIND_DELTA: return run_digit_prescan_scan<KIND_DELTA>(c);
+    case KIND_DIV: return run_digit_prescan_scan<KIND_DIV>(c);
+    case KIND_BITS: return run_digit_prescan_scan<KIND_BITS>(c);
+    case KIND_RANGE: return run_digit_prescan_scan<KIND_RANGE>(c);
+    case KIND_MASK: return run_digit_prescan_scan<KIND_MASK>(c);
+    case KIND_EVEN_FLOAT: return run_digit_prescan_scan<KIND_EVEN_FLOAT>(c);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t dispatch_big_histogram(int kind, const uint32_t* keys, uint32_t n, const BucketParams& p, uint32_t* hist,
+                                   cudaStream_t s) {
+  switch (kind) {
+    case KIND_DELTA: return run_big_histogram<KIND_DELTA>(keys, n, p, hist, s);
+    case KIND_DIV: return run_big_histogram<KIND_DIV>(keys, n, p, hist, s);
+    case KIND_BITS: return run_big_histogram<KIND_BITS>(keys, n, p, hist, s);
+    case KIND_RANGE: return run_big_histogram<KIND_RANGE>(keys, n, p, hist, s);
+    case KIND_MASK: return run_big_histogram<KIND_MASK>(keys, n, p, hist, s);
+    case KIND_EVEN_FLOAT: return run_big_histogram<KIND_EVEN_FLOAT>(keys, n, p, hist, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+gms_status multisplit_big_impl(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n,
+                               const gms_bucket_desc* desc, bool kv, void* scratch, size_t scratch_bytes,
+                               uint32_t* h_offsets, cudaStream_t stream) {
+  gms_status st = check_big_desc(desc);
+  if (st != GMS_SUCCESS) return st;
+  const uint32_t B = desc->num_buckets;
+  if (n == 0) {
+    if (h_offsets)
+      for (uint32_t b = 0; b < B; ++b) h_offsets[b] = 0;
+    return GMS_SUCCESS;
+  }
+  if (scratch == nullptr || (reinterpret_cast<uintptr_t>(scratch) & 255u) != 0) return GMS_ERROR_INVALID_VALUE;
+  if (kin == nullptr || kout == nullptr || overlaps(kin, kout, n)) return GMS_ERROR_INVALID_VALUE;
+  if (kv && (vin == nullptr || vout == nullptr || overlaps(vin, vout, n) || overlaps(kout, vout, n)))
+    return GMS_ERROR_INVALID_VALUE;
+  const BigLayout L = big_layout(n, B, kv);
+  if (scratch_bytes < L.bytes) return GMS_ERROR_SCRATCH_TOO_SMALL;
+  auto* base = static_cast<unsigned char*>(scratch);
+  auto* tk = reinterpret_cast<uint32_t*>(base + L.off_keys);
+  auto* tv = kv ? reinterpret_cast<uint32_t*>(base + L.off_vals) : nullptr;
+  const BucketParams bp = to_params(desc);
+  for (int pass = 0; pass < 2; ++pass) {
+    DigitPass c;
+    c.kin = pass == 0 ? kin : tk;
+    c.vin = kv ? (pass == 0 ? vin : tv) : nullptr;
+    c.kout = pass == 0 ? tk : kout;
+    c.vout = kv ? (pass == 0 ? tv : vout) : nullptr;
+    c.n = n;
+    c.logb = pass == 0 ? 8 : L.logb_hi;
+    c.kv = kv;
+    c.bp.base = bp;
+    c.bp.digit_shift = pass == 0 ? 0u : 8u;
+    c.scratch = base;
+    c.bucket_bytes = base + make_geometry(n, c.logb, kv).off_buckets;
+    c.stream = stream;
+    cudaError_t e = dispatch_digit_prescan(desc->kind, c);
+    if (e == cudaSuccess) e = run_digit_postscan(c);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  if (h_offsets == nullptr) return GMS_SUCCESS;
+  auto* hist = reinterpret_cast<uint32_t*>(base + L.off_hist);
+  cudaError_t e = cudaMemsetAsync(hist, 0, size_t(B) * 4, stream);
+  if (e == cudaSuccess) e = dispatch_big_histogram(desc->kind, kin, n, bp, hist, stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_offsets, hist, size_t(B) * 4, cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  uint32_t run = 0;
+  for (uint32_t b = 0; b < B; ++b) {
+    const uint32_t c = h_offsets[b];
+    h_offsets[b] = run;
+    run += c;
+  }
+  return GMS_SUCCESS;
+}
+
 // ------------------------------------------------ 64-bit keys and values
 // key_bytes 4 or 8; value_bytes 0 (key-only), 4 or 8.
 bool valid_widths(int key_bytes, int value_bytes) {
@@ -512,7 +645,9 @@ const char* gms_status_string(gms_status s) {
   switch (s) {
     case GMS_SUCCESS: return "success";
     case GMS_ERROR_INVALID_VALUE: return "invalid value";
-    case GMS_ERROR_UNSUPPORTED_BUCKETS: return "number of buckets must be in [2, 256] (a power of two for bit-field buckets)";
+    case GMS_ERROR_UNSUPPORTED_BUCKETS:
+      return "unsupported number of buckets: 2..256, up to 65536 for the one-call multisplit and the histogram "
+             "(8192 range splitters), a power of two for bit-field buckets";
     case GMS_ERROR_SCRATCH_TOO_SMALL: return "scratch buffer too small";
     case GMS_ERROR_CUDA: return "CUDA runtime error";
     case GMS_ERROR_DEVICE_TIMEOUT: return "device-side wait timed out";
@@ -535,6 +670,10 @@ gms_status gms_multisplit_scratch_bytes(uint32_t max_elements, uint32_t num_buck
                                         size_t* bytes) {
   int logb = 0;
   if (bytes == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (num_buckets > 256 && num_buckets <= BIG_MAX_BUCKETS) {
+    *bytes = big_layout(max_elements, num_buckets, key_value != 0).bytes;
+    return GMS_SUCCESS;
+  }
   if (!valid_buckets(num_buckets, &logb)) return GMS_ERROR_UNSUPPORTED_BUCKETS;
   *bytes = make_geometry(max_elements, logb, key_value != 0).bytes_full;
   return GMS_SUCCESS;
@@ -554,6 +693,9 @@ gms_status gms_multisplit_geometry(uint32_t n, uint32_t num_buckets, int key_val
 gms_status gms_multisplit_key_only(const uint32_t* d_key_in, uint32_t* d_key_out, uint32_t n,
                                    const gms_bucket_desc* desc, void* d_scratch, size_t scratch_bytes,
                                    uint32_t* h_offsets, gms_stream_t stream) {
+  if (is_big(desc))
+    return multisplit_big_impl(d_key_in, nullptr, d_key_out, nullptr, n, desc, false, d_scratch, scratch_bytes,
+                               h_offsets, stream);
   gms_status st = multisplit_impl(d_key_in, nullptr, d_key_out, nullptr, n, desc, false, d_scratch, scratch_bytes,
                                   STAGE_ALL, stream);
   if (st != GMS_SUCCESS || h_offsets == nullptr) return st;
@@ -566,6 +708,9 @@ gms_status gms_multisplit_key_value(const uint32_t* d_key_in, const uint32_t* d_
                                     uint32_t* d_value_out, uint32_t n, const gms_bucket_desc* desc,
                                     void* d_scratch, size_t scratch_bytes, uint32_t* h_offsets,
                                     gms_stream_t stream) {
+  if (is_big(desc))
+    return multisplit_big_impl(d_key_in, d_value_in, d_key_out, d_value_out, n, desc, true, d_scratch,
+                               scratch_bytes, h_offsets, stream);
   gms_status st = multisplit_impl(d_key_in, d_value_in, d_key_out, d_value_out, n, desc, true, d_scratch,
                                   scratch_bytes, STAGE_ALL, stream);
   if (st != GMS_SUCCESS || h_offsets == nullptr) return st;
@@ -672,6 +817,15 @@ gms_status gms_compaction_key_value(const uint32_t* d_key_in, const uint32_t* d_
 
 gms_status gms_histogram(const uint32_t* d_key_in, uint32_t n, const gms_bucket_desc* desc, int32_t* d_hist,
                          gms_stream_t stream) {
+  if (is_big(desc)) {
+    gms_status st = check_big_desc(desc);
+    if (st != GMS_SUCCESS) return st;
+    if (d_hist == nullptr) return GMS_ERROR_INVALID_VALUE;
+    if (n == 0) return GMS_SUCCESS;
+    if (d_key_in == nullptr) return GMS_ERROR_INVALID_VALUE;
+    return cuda_status(dispatch_big_histogram(desc->kind, d_key_in, n, to_params(desc),
+                                              reinterpret_cast<uint32_t*>(d_hist), stream));
+  }
   int logb = 0;
   gms_status st = check_desc(desc, &logb);
   if (st != GMS_SUCCESS) return st;

@@ -414,6 +414,126 @@ struct DescPolicy64 {
   __device__ __forceinline__ static Id make(const Params& p, const uint32_t* s) { return Id{p, s}; }
 };
 
+// ------------------------------------------- more than 256 buckets
+// B from 257 to 65536 (RANGE: to GMS_RANGE_BIG_MAX splitters) runs as two
+// stable multisplits on the digits of the bucket id, least significant first:
+// the low 8 bits, then id >> 8.  Stable passes make the result the
+// multisplit by the whole id.  DigitId returns digit (id >> shift) of the id.
+#ifndef GMS_RANGE_BIG_MAX
+#define GMS_RANGE_BIG_MAX 8192
+#endif
+constexpr uint32_t BIG_MAX_BUCKETS = 65536;
+
+struct BucketParamsBig {
+  BucketParams base;     // base.num_buckets = B, the whole bucket count
+  uint32_t digit_shift;  // 0 for the low digit, 8 for the high one
+};
+
+// Shared words of the full identifier: RANGE keeps up to GMS_RANGE_BIG_MAX
+// splitters, then a table over the key's top RANGE_LUT_BITS bits (entry t =
+// lo(t) | lo(t+1) << 16, lo(t) the splitters below the cell's first key).
+template <int KIND>
+__host__ __device__ constexpr uint32_t big_identifier_smem_words() {
+  return KIND == KIND_RANGE ? GMS_RANGE_BIG_MAX + RANGE_LUT_CELLS : 1u;
+}
+
+// The whole bucket id of a key, in [0, B).
+template <int KIND>
+__device__ __forceinline__ uint32_t big_bucket_id(uint32_t key, const BucketParams& p, const uint32_t* s_split) {
+  const uint32_t B = p.num_buckets;
+  if constexpr (KIND == KIND_DELTA) {
+    return __umulhi(key, B);
+  } else if constexpr (KIND == KIND_DIV) {
+    return reduce_mod(key / p.param, B);
+  } else if constexpr (KIND == KIND_BITS) {
+    return (key >> p.shift) & (B - 1);
+  } else if constexpr (KIND == KIND_RANGE) {
+    const uint32_t e = s_split[GMS_RANGE_BIG_MAX + (key >> (32 - RANGE_LUT_BITS))];
+    uint32_t c = e & 0xFFFFu, hi = e >> 16;
+    while (c < hi) {  // upper_bound over the cell's splitters
+      const uint32_t mid = (c + hi) >> 1;
+      if (s_split[mid] <= key)
+        c = mid + 1;
+      else
+        hi = mid;
+    }
+    return c == 0u ? B - 1u : c - 1u;
+  } else if constexpr (KIND == KIND_MASK) {
+    return (key & p.param) ? 1u : 0u;
+  } else {  // KIND_EVEN_FLOAT
+    const float x = __fmul_rn(__uint2float_rn(key - p.lower), p.inverse_delta);
+    return reduce_mod(__float2uint_rz(x), B);
+  }
+}
+
+// Fill the full identifier's shared area (RANGE: B splitters and the table).
+// All threads call; a barrier must follow.
+template <int KIND>
+__device__ __forceinline__ void prepare_big_identifier(uint32_t* s_split, const BucketParams& p) {
+  if constexpr (KIND == KIND_RANGE) {
+    const uint32_t B = p.num_buckets;
+    for (uint32_t i = threadIdx.x; i < B; i += blockDim.x) s_split[i] = p.splitters[i];
+    __syncthreads();
+    uint32_t* lut = s_split + GMS_RANGE_BIG_MAX;
+    for (uint32_t t = threadIdx.x; t < RANGE_LUT_CELLS; t += blockDim.x) {
+      auto below = [&](uint32_t v) {  // splitters < v
+        uint32_t lo = 0, hi = B;
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (s_split[mid] < v)
+            lo = mid + 1;
+          else
+            hi = mid;
+        }
+        return lo;
+      };
+      const uint32_t a = below(t << (32 - RANGE_LUT_BITS));
+      const uint32_t b = t + 1 == RANGE_LUT_CELLS ? B : below((t + 1) << (32 - RANGE_LUT_BITS));
+      lut[t] = a | (b << 16);
+    }
+  }
+}
+
+template <int KIND, int LOGB>
+struct DigitId {
+  BucketParams p;
+  uint32_t shift;
+  const uint32_t* s_split;
+  __device__ __forceinline__ uint32_t operator()(uint32_t key) const {
+    return (big_bucket_id<KIND>(key, p, s_split) >> shift) & ((1u << LOGB) - 1u);
+  }
+};
+
+// Policy of one digit pass: the digit is computed once, in the prescan, and
+// kept as a byte for the postscan.
+template <int KIND, int LOGB>
+struct DigitPolicy {
+  using Params = BucketParamsBig;
+  using Id = DigitId<KIND, LOGB>;
+  static constexpr bool CHEAP = false;
+  static constexpr bool USES_SMEM = KIND == KIND_RANGE;
+  static constexpr uint32_t SMEM_WORDS = big_identifier_smem_words<KIND>();
+  __device__ __forceinline__ static void prepare(uint32_t* s, const Params& p) {
+    prepare_big_identifier<KIND>(s, p.base);
+  }
+  __device__ __forceinline__ static Id make(const Params& p, const uint32_t* s) { return Id{p.base, p.digit_shift, s}; }
+};
+
+// The postscan of a digit pass reads the prescan's bytes only; one policy
+// serves every identifier kind.
+struct GivenBytesId {
+  __device__ __forceinline__ uint32_t operator()(uint32_t) const { return 0u; }
+};
+struct GivenBytesPolicy {
+  using Params = BucketParamsBig;
+  using Id = GivenBytesId;
+  static constexpr bool CHEAP = false;
+  static constexpr bool USES_SMEM = false;
+  static constexpr uint32_t SMEM_WORDS = 1;
+  __device__ __forceinline__ static void prepare(uint32_t*, const Params&) {}
+  __device__ __forceinline__ static Id make(const Params&, const uint32_t*) { return Id{}; }
+};
+
 // A user functor (operator() on a 32-bit key, returning the bucket); its
 // value is reduced modulo B like every other identifier.
 template <class F, int LOGB>

@@ -35,4 +35,18 @@ __global__ void __launch_bounds__(HIST_THREADS) histogram_kernel(const uint32_t*
   if (threadIdx.x < num_bins && total) atomicAdd(&hist[threadIdx.x], int32_t(total));
 }
 
+// Histogram over B > 256 bins (to 65536): the whole bucket id of every key
+// (big_bucket_id) added with one global atomic per key into hist[0..B).
+// Persistent grid, strided over keys.
+template <int KIND>
+__global__ void __launch_bounds__(HIST_THREADS) big_histogram_kernel(const uint32_t* __restrict__ keys, uint32_t n,
+                                                                     BucketParams p, uint32_t* __restrict__ hist) {
+  __shared__ uint32_t s_split[big_identifier_smem_words<KIND>()];
+  prepare_big_identifier<KIND>(s_split, p);
+  __syncthreads();
+  const uint32_t stride = gridDim.x * HIST_THREADS;
+  for (uint32_t i = blockIdx.x * HIST_THREADS + threadIdx.x; i < n; i += stride)
+    atomicAdd(&hist[big_bucket_id<KIND>(keys[i], p, s_split)], 1u);
+}
+
 }  // namespace gms

@@ -305,12 +305,91 @@ cudaError_t run_histogram(const uint32_t* keys, uint32_t n, int logb, const Buck
   }
 }
 
+// ------------------------------------------- more than 256 buckets
+template <int KIND, int LOGB, bool KV>
+cudaError_t digit_prescan_scan_t(const DigitPass& c) {
+  using S = TileShape<LOGB, KV>;
+  using C = TileCfg<LOGB, S::WARPS, S::IPT, KV>;
+  const Geometry g = make_geometry(c.n, LOGB, KV);
+  if (g.num_tiles == 0) return cudaSuccess;
+  if (c.bucket_bytes == nullptr) return cudaErrorInvalidValue;
+  auto* hdr = reinterpret_cast<ScratchHeader*>(c.scratch);
+  auto* status = reinterpret_cast<uint64_t*>(c.scratch + g.off_status);
+  auto* matrix = reinterpret_cast<uint32_t*>(c.scratch + g.off_matrix);
+  static std::atomic<int> per_sm{0};
+  auto kern = prescan_kernel<C, DigitPolicy<KIND, LOGB>>;
+  const uint32_t grid = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm);
+  kern<<<grid, C::THREADS, 0, c.stream>>>(c.kin, c.n, g.num_tiles, matrix, c.bp, hdr, status, g.num_chunks,
+                                          c.bucket_bytes);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return run_scan(matrix, g.m, status, hdr, c.stream);
+}
+
+template <int LOGB, bool KV>
+cudaError_t digit_postscan_t(const DigitPass& c) {
+  using S = TileShape<LOGB, KV>;
+  using C = TileCfg<LOGB, S::WARPS, S::IPT, KV>;
+  using P = GivenBytesPolicy;
+  const Geometry g = make_geometry(c.n, LOGB, KV);
+  if (g.num_tiles == 0) return cudaSuccess;
+  if (c.bucket_bytes == nullptr) return cudaErrorInvalidValue;
+  auto* hdr = reinterpret_cast<ScratchHeader*>(c.scratch);
+  auto* matrix = reinterpret_cast<uint32_t*>(c.scratch + g.off_matrix);
+  static std::atomic<uint64_t> smem_done{0};
+  static std::atomic<int> per_sm{0};
+  auto kern = postscan_kernel<C, P, true>;
+  constexpr size_t smem = PostLayout<C, P, true>::BYTES;
+  cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
+  if (e != cudaSuccess) return e;
+  const uint32_t wave = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
+  const uint32_t dist = (GMS_PREFETCH_WAVES * wave) / 4u;
+  kern<<<g.num_tiles, C::THREADS, smem, c.stream>>>(c.kin, c.vin, c.kout, c.vout, c.n, g.num_tiles, matrix, c.bp,
+                                                      hdr, dist, c.bucket_bytes);
+  return cudaGetLastError();
+}
+
+#define GMS_DIGIT_SWITCH(FN, ...)                                 \
+  switch (c.logb) {                                               \
+    case 1: return c.kv ? FN<__VA_ARGS__ 1, true>(c) : FN<__VA_ARGS__ 1, false>(c); \
+    case 2: return c.kv ? FN<__VA_ARGS__ 2, true>(c) : FN<__VA_ARGS__ 2, false>(c); \
+    case 3: return c.kv ? FN<__VA_ARGS__ 3, true>(c) : FN<__VA_ARGS__ 3, false>(c); \
+    case 4: return c.kv ? FN<__VA_ARGS__ 4, true>(c) : FN<__VA_ARGS__ 4, false>(c); \
+    case 5: return c.kv ? FN<__VA_ARGS__ 5, true>(c) : FN<__VA_ARGS__ 5, false>(c); \
+    case 6: return c.kv ? FN<__VA_ARGS__ 6, true>(c) : FN<__VA_ARGS__ 6, false>(c); \
+    case 7: return c.kv ? FN<__VA_ARGS__ 7, true>(c) : FN<__VA_ARGS__ 7, false>(c); \
+    case 8: return c.kv ? FN<__VA_ARGS__ 8, true>(c) : FN<__VA_ARGS__ 8, false>(c); \
+    default: return cudaErrorInvalidValue;                        \
+  }
+
+template <int KIND>
+cudaError_t run_digit_prescan_scan(const DigitPass& c) {
+  GMS_DIGIT_SWITCH(digit_prescan_scan_t, KIND,)
+}
+
+template <int KIND>
+cudaError_t run_big_histogram(const uint32_t* keys, uint32_t n, const BucketParams& p, uint32_t* hist,
+                              cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  static std::atomic<int> per_sm{0};
+  auto kern = big_histogram_kernel<KIND>;
+  const uint32_t grid = persistent_grid(kern, HIST_THREADS, uint32_t((uint64_t(n) + HIST_THREADS - 1) / HIST_THREADS),
+                                        per_sm);
+  kern<<<grid, HIST_THREADS, 0, stream>>>(keys, n, p, hist);
+  return cudaGetLastError();
+}
+
 }  // namespace gms
 
 #define GMS_INSTANTIATE_KIND(K)                                                                        \
   template cudaError_t gms::run_multisplit<K>(const gms::MsCall&, int);                                \
   template cudaError_t gms::run_histogram<K>(const uint32_t*, uint32_t, int, const gms::BucketParams&, \
                                              int32_t*, cudaStream_t);
+
+#define GMS_INSTANTIATE_BIG(K)                                                           \
+  template cudaError_t gms::run_digit_prescan_scan<K>(const gms::DigitPass&);           \
+  template cudaError_t gms::run_big_histogram<K>(const uint32_t*, uint32_t, const gms::BucketParams&, uint32_t*, \
+                                                 cudaStream_t);
 
 #define GMS_INSTANTIATE_WIDE(K) template cudaError_t gms::run_multisplit_wide<K>(const gms::MsCallWide&, int);
 

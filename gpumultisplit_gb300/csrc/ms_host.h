@@ -160,6 +160,35 @@ struct MsCallWide {
 template <int KIND>
 cudaError_t run_multisplit_wide(const MsCallWide& c, int stages);
 
+// One digit pass of a multisplit with more than 256 buckets (32-bit keys and
+// values): 2^logb buckets of digit (id >> bp.digit_shift); the scratch is laid
+// out as make_geometry(n, logb, kv) and bucket_bytes holds n bytes.
+struct DigitPass {
+  const uint32_t* kin = nullptr;
+  const uint32_t* vin = nullptr;
+  uint32_t* kout = nullptr;
+  uint32_t* vout = nullptr;
+  uint32_t n = 0;
+  int logb = 8;
+  bool kv = false;
+  BucketParamsBig bp{};
+  unsigned char* scratch = nullptr;
+  uint8_t* bucket_bytes = nullptr;
+  cudaStream_t stream = nullptr;
+};
+
+// Prescan (identifier evaluated, digit kept as a byte) and scan of a digit
+// pass; defined per kind in inst_big.cu.
+template <int KIND>
+cudaError_t run_digit_prescan_scan(const DigitPass& c);
+// Postscan of a digit pass from the bytes (inst_big_post.cu).
+cudaError_t run_digit_postscan(const DigitPass& c);
+// Adds the count of every whole bucket id in [0, p.num_buckets) into hist
+// (inst_big.cu).
+template <int KIND>
+cudaError_t run_big_histogram(const uint32_t* keys, uint32_t n, const BucketParams& p, uint32_t* hist,
+                              cudaStream_t stream);
+
 // Histogram of keys[0..n) into hist[0..2^logb), accumulated with atomics.
 template <int KIND>
 cudaError_t run_histogram(const uint32_t* keys, uint32_t n, int logb, const BucketParams& bp, int32_t* hist,

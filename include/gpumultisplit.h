@@ -35,7 +35,7 @@ typedef struct CUstream_st* gms_stream_t;
 typedef enum gms_status {
   GMS_SUCCESS = 0,
   GMS_ERROR_INVALID_VALUE = 1,       /* null pointer, bad kind, n over capacity ... */
-  GMS_ERROR_UNSUPPORTED_BUCKETS = 2, /* num_buckets outside [2, 256], or not a power of two for BITS */
+  GMS_ERROR_UNSUPPORTED_BUCKETS = 2, /* num_buckets outside what the call takes, or not a power of two for BITS */
   GMS_ERROR_SCRATCH_TOO_SMALL = 3,
   GMS_ERROR_CUDA = 4,                /* a CUDA runtime call failed; see gms_last_cuda_error() */
   GMS_ERROR_DEVICE_TIMEOUT = 5,      /* a bounded device-side wait gave up (read by gms_read_device_error) */
@@ -52,6 +52,13 @@ typedef enum gms_status {
  * for those every kind gives the same buckets as below).  The kernels then
  * run with the next power of two and leave the buckets from B up empty.
  * BITS needs a power of two.  Offsets and histograms hold B entries.
+ *
+ * gms_multisplit_key_only / _key_value, gms_multisplit_scratch_bytes and
+ * gms_histogram also take B from 257 to 65536 (RANGE: up to 8192 splitters).
+ * The multisplit then runs as two stable multisplits on the digits of the
+ * bucket id (id & 255, then id >> 8), through buffers in the scratch; the
+ * result is the same stable order.  The stage entry points, the batched and
+ * serving forms and the 64-bit entry points take B <= 256.
  *
  *  GMS_BUCKET_DELTA       key * B >> 32 (64-bit product): B equal-width key ranges.
  *  GMS_BUCKET_DIV         (key / param) mod B (delta_func, README.md:85-91, src/main/main_multisplit.cu:41-47).
@@ -77,7 +84,7 @@ typedef enum gms_bucket_kind {
 
 typedef struct gms_bucket_desc {
   int32_t kind;                /* gms_bucket_kind */
-  uint32_t num_buckets;        /* B: 2..256 (a power of two for BITS) */
+  uint32_t num_buckets;        /* B: 2..256, to 65536 where noted (a power of two for BITS) */
   uint32_t shift;              /* BITS */
   uint32_t param;              /* DIV: divisor (non-zero); MASK: mask */
   uint32_t lower;              /* EVEN_FLOAT: lower level */

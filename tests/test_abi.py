@@ -68,7 +68,7 @@ def test_scratch_and_geometry(gms_lib, B, kv):
 
 
 def test_unsupported_bucket_counts(gms_lib):
-    for B in (0, 1, 257, 512):
+    for B in (0, 1, 65537, 1 << 20):
         st, _ = scratch_bytes(100, B, 0)
         assert st == _lib.GMS_ERROR_UNSUPPORTED_BUCKETS
     # any count in [2, 256] is taken (the kernels round it up to a power of two) ...
@@ -83,9 +83,23 @@ def test_unsupported_bucket_counts(gms_lib):
 
 def test_argument_checks_before_cuda(gms_lib):
     """These calls fail on their arguments, before any CUDA work."""
-    d = _lib.BucketDesc(kind=_lib.GMS_BUCKET_DELTA, num_buckets=300)
+    d = _lib.BucketDesc(kind=_lib.GMS_BUCKET_DELTA, num_buckets=70000)
     assert gms_lib.gms_multisplit_key_only(1 << 20, 2 << 20, 10, ctypes.byref(d), 1 << 24, 1 << 20, None,
                                            None) == _lib.GMS_ERROR_UNSUPPORTED_BUCKETS
+    # more than 256 buckets: RANGE to 8192 splitters, BITS a power of two, not through the stage calls
+    for kind, B, want in ((_lib.GMS_BUCKET_RANGE, 8193, _lib.GMS_ERROR_UNSUPPORTED_BUCKETS),
+                          (_lib.GMS_BUCKET_BITS, 1000, _lib.GMS_ERROR_UNSUPPORTED_BUCKETS),
+                          (_lib.GMS_BUCKET_DIV, 1000, _lib.GMS_ERROR_INVALID_VALUE)):
+        d = _lib.BucketDesc(kind=kind, num_buckets=B, d_splitters=1 << 26)
+        assert gms_lib.gms_multisplit_key_value(1 << 20, 2 << 20, 3 << 20, 4 << 20, 10, ctypes.byref(d), 1 << 24,
+                                                1 << 26, None, None) == want
+    d = _lib.BucketDesc(kind=_lib.GMS_BUCKET_DELTA, num_buckets=1000)
+    assert gms_lib.gms_multisplit_prescan(1 << 20, 10, ctypes.byref(d), 1, 1 << 24, 1 << 26, None) == \
+        _lib.GMS_ERROR_UNSUPPORTED_BUCKETS
+    need = ctypes.c_size_t()
+    assert gms_lib.gms_multisplit_scratch_bytes(100000, 1000, 1, ctypes.byref(need)) == 0
+    assert gms_lib.gms_multisplit_key_value(1 << 20, 2 << 21, 3 << 21, 4 << 21, 100000, ctypes.byref(d), 1 << 24,
+                                            need.value - 256, None, None) == _lib.GMS_ERROR_SCRATCH_TOO_SMALL
     d = _lib.BucketDesc(kind=99, num_buckets=8)
     assert gms_lib.gms_multisplit_key_only(1 << 20, 2 << 20, 10, ctypes.byref(d), 1 << 24, 1 << 20, None,
                                            None) == _lib.GMS_ERROR_INVALID_VALUE

@@ -179,7 +179,7 @@ def test_repeated_calls_reuse_scratch(gms_lib, oracle_mod):
 
 
 def test_errors_are_reported(gms_lib):
-    ctx = gms.multisplit_context(300)
+    ctx = gms.multisplit_context(70000)
     with pytest.raises(gms.GmsError):
         gms.multisplit_allocate_key_only(100, ctx)
     ctx = gms.multisplit_context(16)

@@ -209,3 +209,25 @@ def test_oracle_64bit_keys_against_numpy(oracle_mod):
     ks, vs = o.sort_bits64(keys, vals.astype(np.uint32), 13, 47, 7)
     sub = (keys >> np.uint64(13)) & np.uint64((1 << 34) - 1)
     assert np.array_equal(vs, vals.astype(np.uint32)[np.argsort(sub, kind="stable")])
+
+
+def test_oracle_more_than_256_buckets(oracle_mod):
+    """B above 256: the oracle's ids and order against numpy, and against the
+    reference's CPU multisplit where it is built (it takes any bucket count)."""
+    o = oracle_mod
+    keys = datagen.as_u32(datagen.uniform_u32(20000, 41))
+    keys[:3] = [0, 0xFFFFFFFF, 0x80000000]
+    vals = np.arange(keys.size, dtype=np.uint32)
+    for B in (257, 1000, 4096, 65536):
+        spl = np.concatenate([[0], np.sort(datagen.as_u32(datagen.uniform_u32(B - 1, B)))]).astype(np.uint32)
+        ub = np.searchsorted(spl, keys, side="right").astype(np.int64) - 1
+        for d, ids in ((o.Desc(o.DELTA, B), (keys.astype(np.uint64) * B) >> 32),
+                       (o.Desc(o.RANGE, B, splitters=spl), np.where(ub < 0, B - 1, ub)),
+                       (o.Desc(o.DIV, B, param=4099), (keys // 4099) % B)):
+            ko, vo, offs = o.multisplit(keys, d, vals)
+            order = np.argsort(ids, kind="stable")
+            assert np.array_equal(ko, keys[order]) and np.array_equal(vo, order)
+            assert np.array_equal(offs, np.searchsorted(np.sort(ids), np.arange(B)).astype(np.uint32))
+            if o.ref_available():
+                rk, rv = o.ref_multisplit(keys, d, vals)
+                assert np.array_equal(rk, ko) and np.array_equal(rv, vo)
