@@ -65,8 +65,9 @@ def parse():
     p.add_argument("--only-serving", action="store_true", help="print only the serving-form summary")
     p.add_argument("--serve-seconds", type=float, default=3.0)
     p.add_argument("--serve-rate", type=float, default=20000.0)
-    p.add_argument("--sweep-wide", action="store_true",
-                   help="with --sweep: only the 64-bit key / value cases")
+    p.add_argument("--sweep-part", default="all", choices=["all", "base", "wide", "big"],
+                   help="with --sweep: all cases, or only the 32-bit cases (base), the 64-bit key / value cases "
+                        "(wide) or the cases with more than 256 buckets (big)")
     p.add_argument("--sweep", action="store_true",
                    help="time every 2^28 case of the key-value sweep, key-only, compaction, histogram and sort "
                         "(one JSON line per case) instead of the headline line")
@@ -315,7 +316,7 @@ def run_sweep(a, dev):
 
     n = 1 << a.log2n
     peak, _ = hbm_peak()
-    inputs = {} if a.sweep_wide else {"uniform": datagen.uniform_u32(n, 3, device=dev),
+    inputs = {} if a.sweep_part in ("wide", "big") else {"uniform": datagen.uniform_u32(n, 3, device=dev),
                                       "zipf": datagen.zipf_u32(n, 3, device=dev),
                                       "and4": datagen.and4_u32(n, 3, device=dev)}
     vals = datagen.index_values(n, dev)
@@ -380,7 +381,7 @@ def run_sweep(a, dev):
             ok &= bool((vo[1:][same] > vo[:-1][same]).all())  # stable: values = input index
         return "pass" if ok else "FAIL"
 
-    if not a.sweep_wide:
+    if a.sweep_part in ("all", "base"):
         # key-value sweep: B x distribution x identifier
         for dist in ("uniform", "zipf"):
             for ident_name in ("delta", "range"):
@@ -460,11 +461,24 @@ def run_sweep(a, dev):
                     emit(f"sort {bits}-bit {'kv' if kv else 'k'} {dist}", ms, passes * (20 if kv else 12),
                          "pass" if ok else "FAIL", cpu_rate(lambda: oracle.sort(hk, hv, bits), 1))
                     gms.multisplit_sort_release_memory(ctx)
-    # 64-bit keys and values: multisplit (B = 256, delta on the 64-bit key) and
-    # sorts.  Algorithmic bytes: prescan reads the key, postscan reads and
-    # writes key and value (the bucket bytes, 2 B/key, are not counted).
     del inputs, kout, vout
     torch.cuda.empty_cache()
+    if a.sweep_part in ("all", "wide"):
+        sweep_wide(n, dev, timed, emit, cpu_rate, sample, sample_n)
+    if a.sweep_part in ("all", "big"):
+        sweep_big(n, dev, timed, emit, cpu_rate, sample)
+
+
+def sweep_wide(n, dev, timed, emit, cpu_rate, sample, sample_n):
+    """64-bit keys and values: multisplit (B = 256, delta on the 64-bit key) and
+    sorts.  Algorithmic bytes: prescan reads the key, postscan reads and writes
+    key and value (the bucket bytes, 2 B/key, are not counted)."""
+    import torch
+
+    import gpumultisplit_gb300 as gms
+    import oracle
+    from gpumultisplit_gb300 import datagen
+
     k64 = datagen.uniform_u64(n, 3, device=dev)
     k32 = datagen.uniform_u32(n, 3, device=dev)
     v64 = torch.arange(n, dtype=torch.int64, device=dev)
@@ -519,6 +533,41 @@ def run_sweep(a, dev):
              cpu_rate(lambda: oracle.sort_bits64(hk, hv, 0, 64, 8), 1))
         del ctx, ko, vo
 
+
+def sweep_big(n, dev, timed, emit, cpu_rate, sample):
+    """More than 256 buckets: two digit passes, each with the traffic of a
+    multisplit plus its bucket bytes; the algorithmic bytes are those of one
+    multisplit (20 B/pair), so the HBM fraction shows the cost of the second
+    pass."""
+    import torch
+
+    import gpumultisplit_gb300 as gms
+    import oracle
+    from gpumultisplit_gb300 import datagen
+
+    kin = datagen.uniform_u32(n, 3, device=dev)
+    vin = datagen.index_values(n, dev)
+    kout, vout = torch.empty_like(kin), torch.empty_like(vin)
+    for B, ident_name in ((1000, "delta"), (4096, "delta"), (4096, "range"), (65536, "delta")):
+        spl = datagen.range_splitters(B, 5, dev) if ident_name == "range" else None
+        ident = gms.delta_bucket() if spl is None else gms.range_bucket(spl)
+        ctx = gms.multisplit_context(B)
+        gms.multisplit_allocate_key_value(n, ctx)
+        ms = timed(lambda: gms.multisplit_key_value(kin, vin, kout, vout, n, ctx, ident))
+        u = kout.long() & 0xFFFFFFFF
+        if spl is None:
+            b = (u * B) >> 32
+        else:
+            b = torch.searchsorted(spl.long() & 0xFFFFFFFF, u, right=True) - 1
+        same = b[1:] == b[:-1]
+        ok = bool((b[1:] >= b[:-1]).all()) and bool(torch.equal(kin[vout.long()], kout)) and \
+            bool((vout[1:][same] > vout[:-1][same]).all())
+        hk, hv = sample(kin), sample(vin)
+        desc = oracle.Desc(oracle.DELTA if spl is None else oracle.RANGE, B,
+                           splitters=None if spl is None else datagen.as_u32(spl))
+        emit(f"multisplit kv B={B} uniform {ident_name} (two digit passes)", ms, 20, "pass" if ok else "FAIL",
+             cpu_rate(lambda: oracle.multisplit(hk, desc, hv), 1))
+        gms.multisplit_release_memory(ctx)
 
 def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: float = 64.0, verify: int = 24,
                 verify_all: bool = True):
