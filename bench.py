@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline time budget")
     p.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
     p.add_argument("--only-batched", action="store_true", help="print only the batched-form summary")
+    p.add_argument("--only-tiny-segments", action="store_true",
+                   help="print only the many-small-segments summary (one warp per segment against tiles)")
     p.add_argument("--no-autotune", action="store_true",
                    help="batched form: keep the built-in tile table instead of autotuning first")
     p.add_argument("--no-serving", action="store_true", help="skip the serving-form measurement")
@@ -569,6 +571,63 @@ def sweep_big(n, dev, timed, emit, cpu_rate, sample):
              cpu_rate(lambda: oracle.multisplit(hk, desc, hv), 1))
         gms.multisplit_release_memory(ctx)
 
+def run_tiny_segments(dev, count: int = 200000, seed: int = 9):
+    """Many small multisplits: `count` key-value segments of 1..512 keys (uniform
+    sizes, seed), B = 256 delta.  The tuned plan multisplits each segment with
+    one warp in one launch; a forced 1024-key tile shape runs the tiled path
+    (prescan, scan, postscan) on the same segments; the plain per-call loop is
+    timed on a sample of 1000 segments and scaled.  Outputs are compared."""
+    import torch
+
+    import gpumultisplit_gb300 as gms
+    from gpumultisplit_gb300 import datagen
+
+    sizes = np.random.default_rng(seed).integers(1, 513, count)
+    starts = np.concatenate([[0], np.cumsum(sizes)])
+    total = int(starts[-1])
+    keys = datagen.uniform_u32(total, seed, device=dev)
+    vals = datagen.index_values(total, dev)
+    kout, vout = torch.empty_like(keys), torch.empty_like(vals)
+    segs = [gms.Segment(keys[a:b], kout[a:b], int(b - a), 256, gms.delta_bucket(), vals[a:b], vout[a:b])
+            for a, b in zip(starts[:-1].tolist(), starts[1:].tolist())]
+    warp_plan = gms.BatchedMultisplit(segs)
+    tiled_plan = gms.BatchedMultisplit(segs, variant=2)
+
+    def timed(fn, reps=10):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    warp_ms = timed(lambda: warp_plan.run(use_graph=True))
+    ref_k, ref_v = kout.clone(), vout.clone()
+    tiled_ms = timed(lambda: tiled_plan.run(use_graph=True))
+    same = bool(torch.equal(kout, ref_k)) and bool(torch.equal(vout, ref_v))
+    ctx = gms.multisplit_context(256)
+    gms.multisplit_allocate_key_value(512, ctx)
+    sample = segs[:1000]
+
+    def plain():
+        for sg in sample:
+            gms.multisplit_key_value(sg.keys_in, sg.values_in, sg.keys_out, sg.values_out, sg.n, ctx, sg.identifier)
+
+    plain_ms = timed(plain, 3) * count / len(sample)
+    out = {"workload": f"{count} key-value segments of 1..512 keys (uniform sizes, seed {seed}), B = 256 delta; "
+                       f"{total} pairs",
+           "pairs": total, "one_warp_ms": warp_ms, "one_warp_gkeys": total / (warp_ms * 1e-3) / 1e9,
+           "launches": warp_plan.launches, "tiled_ms": tiled_ms, "tiled_gkeys": total / (tiled_ms * 1e-3) / 1e9,
+           "tiled_launches": tiled_plan.launches, "plain_ms_scaled": plain_ms,
+           "plain_gkeys": total / (plain_ms * 1e-3) / 1e9, "identical": same,
+           "device_error": warp_plan.device_error()}
+    warp_plan.close()
+    tiled_plan.close()
+    return out
+
 def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: float = 64.0, verify: int = 24,
                 verify_all: bool = True):
     """Serving form under Poisson arrivals against the plain per-request calls on
@@ -922,12 +981,15 @@ def run_ours(a):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if a.only_batched or a.only_serving:
+    if a.only_batched or a.only_serving or a.only_tiny_segments:
         from gpumultisplit_gb300 import build as gbuild
 
         gbuild.build()
-        out = (run_batched(dev, tune=not a.no_autotune) if a.only_batched
-               else run_serving(dev, a.serve_seconds, a.serve_rate))
+        if a.only_tiny_segments:
+            out = run_tiny_segments(dev)
+        else:
+            out = (run_batched(dev, tune=not a.no_autotune) if a.only_batched
+                   else run_serving(dev, a.serve_seconds, a.serve_rate))
         print(json.dumps(out), flush=True)
         return
     if world > 1:

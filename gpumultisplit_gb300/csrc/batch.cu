@@ -19,9 +19,14 @@ struct BatchClass {
   int kind = 0;
   int logb = 1;
   bool kv = false;
-  int variant = 0;           // tile shape (kTileVariants)
-  std::vector<uint2> tiles;  // (segment, tile)
-  size_t map_off = 0;        // byte offset of this class's map in scratch
+  int variant = 0;                 // tile shape (kTileVariants)
+  bool warp = false;               // segments of at most kWarpSegMax keys, one warp each
+  std::vector<uint2> tiles;        // (segment, tile)
+  std::vector<uint32_t> seg_ids;   // warp classes: their segments
+  size_t map_off = 0;              // byte offset of this class's map (or segment list) in scratch
+  size_t work() const { return warp ? seg_ids.size() / 8 + 1 : tiles.size(); }  // for the launch order
+  const void* map_data() const { return warp ? static_cast<const void*>(seg_ids.data()) : tiles.data(); }
+  size_t map_bytes() const { return warp ? seg_ids.size() * sizeof(uint32_t) : tiles.size() * sizeof(uint2); }
 };
 
 // A run of consecutive segments whose n sum stays below 2^32, scanned on its own.
@@ -82,6 +87,18 @@ cudaError_t dispatch_variant(const BatchClassLaunch& c, int stage) {
 }
 static_assert(kNumTileVariants == 4, "dispatch_variant covers every tile variant");
 
+cudaError_t run_batch_warp_kind(int kind, const BatchClassLaunch& c) {
+  switch (kind) {
+    case KIND_DELTA: return run_batch_warp<KIND_DELTA>(c);
+    case KIND_DIV: return run_batch_warp<KIND_DIV>(c);
+    case KIND_BITS: return run_batch_warp<KIND_BITS>(c);
+    case KIND_RANGE: return run_batch_warp<KIND_RANGE>(c);
+    case KIND_MASK: return run_batch_warp<KIND_MASK>(c);
+    case KIND_EVEN_FLOAT: return run_batch_warp<KIND_EVEN_FLOAT>(c);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 constexpr int kSideStreams = 4;
 
 cudaError_t ensure_side_streams(gms_batch_s* b) {
@@ -120,16 +137,23 @@ cudaError_t launch_classes(gms_batch_s* b, BatchClassLaunch L, unsigned char* sc
   std::vector<size_t> order(nc);
   for (size_t i = 0; i < nc; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(),
-                   [&](size_t x, size_t y) { return b->classes[x].tiles.size() > b->classes[y].tiles.size(); });
+                   [&](size_t x, size_t y) { return b->classes[x].work() > b->classes[y].work(); });
   for (size_t k = 0; k < nc; ++k) {
     const BatchClass& c = b->classes[order[k]];
     L.logb = c.logb;
     L.kv = c.kv;
     L.variant = c.variant;
-    L.tile_map = reinterpret_cast<const uint2*>(scratch + c.map_off);
-    L.class_tiles = uint32_t(c.tiles.size());
     L.stream = lanes > 0 ? b->side[k % size_t(lanes)] : s;
-    e = run_batch_class(c.kind, L, stage);
+    if (c.warp) {  // one kernel does the whole multisplit: launched with the postscans
+      if (stage != STAGE_POSTSCAN) continue;
+      L.seg_ids = reinterpret_cast<const uint32_t*>(scratch + c.map_off);
+      L.class_tiles = uint32_t(c.seg_ids.size());
+      e = run_batch_warp_kind(c.kind, L);
+    } else {
+      L.tile_map = reinterpret_cast<const uint2*>(scratch + c.map_off);
+      L.class_tiles = uint32_t(c.tiles.size());
+      e = run_batch_class(c.kind, L, stage);
+    }
     if (e != cudaSuccess) return e;
   }
   for (int i = 0; e == cudaSuccess && i < lanes; ++i) {
@@ -188,6 +212,7 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
     return GMS_ERROR_INVALID_VALUE;
   auto* b = new gms_batch_s();
   std::map<std::tuple<int, int, bool, int>, size_t> class_index;
+  std::vector<std::pair<uint32_t, int>> warp_segs;  // (segment, log2 B) on the one-warp path
   uint64_t matrix_total = 0, group_n = 0, byte_total = 0;
   ScanGroup group;
   for (uint32_t i = 0; i < count; ++i) {
@@ -223,6 +248,25 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
     d.bp.inverse_delta = sg.desc.inverse_delta;
     d.bp.splitters = sg.desc.d_splitters;
     d.bp.num_buckets = sg.desc.num_buckets;
+    if (variant < 0 && sg.n > 0 && sg.n <= kWarpSegMax) {
+      // One warp multisplits the whole segment; its bucket starts get matrix
+      // entries after every scan group (assigned below).
+      b->segs.push_back(d);
+      warp_segs.emplace_back(i, logb);
+      const auto key = std::make_tuple(kind, logb, kv, -1);
+      auto it = class_index.find(key);
+      if (it == class_index.end()) {
+        it = class_index.emplace(key, b->classes.size()).first;
+        BatchClass c;
+        c.kind = kind;
+        c.logb = logb;
+        c.kv = kv;
+        c.warp = true;
+        b->classes.push_back(c);
+      }
+      b->classes[it->second].seg_ids.push_back(i);
+      continue;
+    }
     const int v = variant >= 0 ? variant : tuned_variant(logb, kv, sg.n);
     if (!variant_valid(v, logb)) {
       delete b;
@@ -272,6 +316,18 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
   }
   group.m = uint32_t(matrix_total - group.matrix_first);
   if (group.m > 0) b->groups.push_back(group);
+  // Bucket starts of the one-warp segments: one tile's entries each, past every group.
+  for (const auto& [i, logb] : warp_segs) {
+    SegDesc& d = b->segs[i];
+    d.num_tiles = 1;
+    d.base = 0;
+    d.matrix_off = uint32_t(matrix_total);
+    matrix_total += uint64_t(1u) << logb;
+    if (matrix_total > 0xFFFFFFFFull) {
+      delete b;
+      return GMS_ERROR_NOT_SUPPORTED;
+    }
+  }
   for (const ScanGroup& g : b->groups)
     b->max_chunks = std::max(b->max_chunks, (g.m + kScanChunk - 1) / kScanChunk);
 
@@ -281,7 +337,7 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
   b->off_maps = off;
   for (BatchClass& c : b->classes) {
     c.map_off = off;
-    off = align_up(off + c.tiles.size() * sizeof(uint2), 256);
+    off = align_up(off + c.map_bytes(), 256);
   }
   b->off_matrix = off;
   off = align_up(off + size_t(matrix_total) * 4, 256);
@@ -317,7 +373,7 @@ gms_status gms_batch_scratch_bytes(gms_batch_t batch, size_t* bytes) {
 gms_status gms_batch_launch_count(gms_batch_t batch, uint32_t* launches) {
   if (batch == nullptr || launches == nullptr) return GMS_ERROR_INVALID_VALUE;
   uint32_t n = 0;
-  for (const BatchClass& c : batch->classes) n += c.tiles.empty() ? 0u : 2u;
+  for (const BatchClass& c : batch->classes) n += c.warp ? 1u : (c.tiles.empty() ? 0u : 2u);
   for (const ScanGroup& g : batch->groups) n += g.m > 0 ? 1u : 0u;
   *launches = n;
   return GMS_SUCCESS;
@@ -338,8 +394,7 @@ gms_status gms_batch_run(gms_batch_t b, void* d_scratch, size_t scratch_bytes, i
                         cudaMemcpyHostToDevice, stream);
     for (size_t i = 0; e == cudaSuccess && i < b->classes.size(); ++i) {
       const BatchClass& c = b->classes[i];
-      e = cudaMemcpyAsync(scratch + c.map_off, c.tiles.data(), c.tiles.size() * sizeof(uint2),
-                          cudaMemcpyHostToDevice, stream);
+      e = cudaMemcpyAsync(scratch + c.map_off, c.map_data(), c.map_bytes(), cudaMemcpyHostToDevice, stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return to_status(e);
@@ -388,7 +443,7 @@ gms_status batch_run_async(gms_batch_t b, void* d_scratch, size_t scratch_bytes,
   auto* staging = static_cast<unsigned char*>(h_pinned);
   std::memcpy(staging, b->segs.data(), b->segs.size() * sizeof(SegDesc));
   for (const BatchClass& c : b->classes)
-    std::memcpy(staging + (c.map_off - b->off_segs), c.tiles.data(), c.tiles.size() * sizeof(uint2));
+    std::memcpy(staging + (c.map_off - b->off_segs), c.map_data(), c.map_bytes());
   auto* scratch = static_cast<unsigned char*>(d_scratch);
   cudaError_t e = cudaMemcpyAsync(scratch + b->off_segs, staging, table, cudaMemcpyHostToDevice, stream);
   if (e == cudaSuccess) e = launch_all(b, scratch, stream);

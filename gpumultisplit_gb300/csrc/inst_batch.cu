@@ -8,3 +8,7 @@
 #endif
 
 GMS_INSTANTIATE_BATCH(GMS_INST_KIND, GMS_INST_VARIANT)
+
+#if GMS_INST_VARIANT == 0
+GMS_INSTANTIATE_BATCH_WARP(GMS_INST_KIND)  // the one-warp-per-segment kernels, once per kind
+#endif

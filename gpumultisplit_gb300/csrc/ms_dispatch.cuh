@@ -273,6 +273,31 @@ cudaError_t run_batch_class_kv(const BatchClassLaunch& c, int stage) {
   }
 }
 
+template <int KIND, int LOGB, bool KV>
+cudaError_t run_batch_warp_t(const BatchClassLaunch& c) {
+  static_assert(kWarpSegMax == WARP_SEG_MAX, "host and kernel agree on the warp segment size");
+  if (c.class_tiles == 0) return cudaSuccess;
+  const uint32_t blocks = (c.class_tiles + WARP_SEG_WARPS - 1) / WARP_SEG_WARPS;
+  batch_warp_kernel<KIND, LOGB, KV><<<blocks, WARP_SEG_WARPS * 32, 0, c.stream>>>(c.segs, c.seg_ids, c.class_tiles,
+                                                                                 c.matrix);
+  return cudaGetLastError();
+}
+
+template <int KIND>
+cudaError_t run_batch_warp(const BatchClassLaunch& c) {
+  switch (c.logb) {
+    case 1: return c.kv ? run_batch_warp_t<KIND, 1, true>(c) : run_batch_warp_t<KIND, 1, false>(c);
+    case 2: return c.kv ? run_batch_warp_t<KIND, 2, true>(c) : run_batch_warp_t<KIND, 2, false>(c);
+    case 3: return c.kv ? run_batch_warp_t<KIND, 3, true>(c) : run_batch_warp_t<KIND, 3, false>(c);
+    case 4: return c.kv ? run_batch_warp_t<KIND, 4, true>(c) : run_batch_warp_t<KIND, 4, false>(c);
+    case 5: return c.kv ? run_batch_warp_t<KIND, 5, true>(c) : run_batch_warp_t<KIND, 5, false>(c);
+    case 6: return c.kv ? run_batch_warp_t<KIND, 6, true>(c) : run_batch_warp_t<KIND, 6, false>(c);
+    case 7: return c.kv ? run_batch_warp_t<KIND, 7, true>(c) : run_batch_warp_t<KIND, 7, false>(c);
+    case 8: return c.kv ? run_batch_warp_t<KIND, 8, true>(c) : run_batch_warp_t<KIND, 8, false>(c);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 template <int KIND, int V>
 cudaError_t run_batch_class_v(const BatchClassLaunch& c, int stage) {
   return c.kv ? run_batch_class_kv<KIND, true, V>(c, stage) : run_batch_class_kv<KIND, false, V>(c, stage);
@@ -392,5 +417,7 @@ cudaError_t run_big_histogram(const uint32_t* keys, uint32_t n, const BucketPara
                                                  cudaStream_t);
 
 #define GMS_INSTANTIATE_WIDE(K) template cudaError_t gms::run_multisplit_wide<K>(const gms::MsCallWide&, int);
+
+#define GMS_INSTANTIATE_BATCH_WARP(K) template cudaError_t gms::run_batch_warp<K>(const gms::BatchClassLaunch&);
 
 #define GMS_INSTANTIATE_BATCH(K, V) template cudaError_t gms::run_batch_class_v<K, V>(const gms::BatchClassLaunch&, int);

@@ -208,6 +208,7 @@ struct BatchClassLaunch {
   uint32_t class_tiles = 0;
   uint32_t* matrix = nullptr;       // device, the batch count matrix
   uint8_t* byte_area = nullptr;     // device, bucket bytes of segments with costly identifiers
+  const uint32_t* seg_ids = nullptr;  // device, segments of a one-warp-per-segment class
   ScratchHeader* hdr = nullptr;
   cudaStream_t stream = nullptr;
 };
@@ -217,6 +218,14 @@ struct BatchClassLaunch {
 // inst_batch.cu.
 template <int KIND, int V>
 cudaError_t run_batch_class_v(const BatchClassLaunch& c, int stage);
+
+// Segments of at most this many keys are multisplit one warp each (tuned plans).
+constexpr uint32_t kWarpSegMax = 512;
+
+// Launches the one-warp-per-segment kernel of a class of small segments:
+// c.seg_ids lists c.class_tiles segments (inst_batch.cu, variant 0 units).
+template <int KIND>
+cudaError_t run_batch_warp(const BatchClassLaunch& c);
 
 // Dispatch on the class's kind and variant (batch.cu).
 cudaError_t run_batch_class(int kind, const BatchClassLaunch& c, int stage);

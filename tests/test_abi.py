@@ -275,7 +275,8 @@ def test_tuning_table_host_logic(gms_lib):
 
 
 def test_batch_plan_classes_follow_the_table(gms_lib):
-    """Plans are host-only: launches = 2 per (kind, B, key/value, variant) class + 1 scan."""
+    """Plans are host-only: launches = 2 per (kind, B, key/value, variant) class + 1 scan,
+    and 1 per class of segments small enough for one warp each."""
     from gpumultisplit_gb300 import batched
 
     gms.reset_tuning()
@@ -302,6 +303,11 @@ def test_batch_plan_classes_follow_the_table(gms_lib):
     gms.set_tuning({(256, True, c): 0 for c in range(8)})
     assert plan([1000, 1500, 5000]) == 2 + 1
     gms.reset_tuning()
+    # segments of at most 512 keys: one warp each, one launch per class, no scan
+    assert plan([100, 512]) == 1
+    assert plan([100, 512, 513]) == 1 + 2 + 1
+    assert plan([100, 7, 0], B=5) == 1
+    assert plan([100, 512], variant=2) == 2 + 1  # a forced tile shape keeps them tiled
     arr = (batched.GmsSegment * 1)()
     arr[0] = batched.GmsSegment(fake, fake, fake, fake, 10, gms.delta_bucket().desc(256))
     h = ctypes.c_void_p()

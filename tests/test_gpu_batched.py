@@ -140,3 +140,74 @@ def test_autotune_fills_table_and_keeps_outputs(gms_lib, oracle_mod):
         plan.close()
     finally:
         gms.reset_tuning()
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_small_segments_one_warp_each(gms_lib, oracle_mod, use_graph):
+    """Segments of at most 512 keys take the one-warp path (one launch per class,
+    no scan); every kind, power-of-two and other bucket counts, key-only and
+    key-value, beside tiled segments: each equals the oracle and the plan with
+    a forced tile shape (the tiled path for every segment)."""
+    o = oracle_mod
+    rng = np.random.default_rng(17)
+    sizes = [1, 2, 31, 32, 33, 100, 255, 256, 257, 511, 512, 513, 1000, 5000] + \
+        [int(x) for x in rng.integers(1, 513, 120)]
+    buckets = (2, 3, 8, 12, 32, 33, 64, 100, 128, 256)
+    segs, refs = [], []
+    for i, n in enumerate(sizes):
+        B = int(buckets[rng.integers(len(buckets))])
+        kind = int(rng.integers(6))
+        if kind == o.BITS and B & (B - 1):
+            kind = o.DELTA  # bit-field buckets are powers of two
+        kv = i % 4 != 1
+        keys = datagen.as_u32(datagen.uniform_u32(n, 3000 + i))
+        vals = np.arange(n, dtype=np.uint32) if kv else None
+        ident, d, keep = identifiers(o, kind, B, splitter_seed=40 + i)
+        segs.append(gms.Segment(to_dev(keys), torch.zeros(n, dtype=torch.int32, device="cuda"), n, B, ident,
+                                to_dev(vals) if kv else None,
+                                torch.zeros(n, dtype=torch.int32, device="cuda") if kv else None))
+        refs.append((keys, vals, d, keep))
+    plan = gms.BatchedMultisplit(segs)
+    plan.run(use_graph=use_graph)
+    torch.cuda.synchronize()
+    assert plan.device_error() == 0
+    check_against_oracle(o, segs, refs)
+    outs = [(s_.keys_out.clone(), None if s_.values_out is None else s_.values_out.clone()) for s_ in segs]
+    plan.close()
+    for s_ in segs:
+        s_.keys_out.zero_()
+        if s_.values_out is not None:
+            s_.values_out.zero_()
+    tiled = gms.BatchedMultisplit(segs, variant=2)
+    tiled.run(use_graph=use_graph)
+    torch.cuda.synchronize()
+    for s_, (k, v) in zip(segs, outs):
+        assert torch.equal(s_.keys_out, k)
+        if v is not None:
+            assert torch.equal(s_.values_out, v)
+    tiled.close()
+
+
+def test_many_tiny_segments(gms_lib, oracle_mod):
+    """20000 segments of 1..512 keys, B = 256 delta, key-value: one launch."""
+    o = oracle_mod
+    rng = np.random.default_rng(5)
+    sizes = rng.integers(1, 513, 20000)
+    total = int(sizes.sum())
+    keys = datagen.uniform_u32(total, 77, device="cuda")
+    vals = torch.arange(total, dtype=torch.int32, device="cuda")
+    kout, vout = torch.empty_like(keys), torch.empty_like(vals)
+    starts = np.concatenate([[0], np.cumsum(sizes)])
+    segs = [gms.Segment(keys[a:b], kout[a:b], int(b - a), 256, gms.delta_bucket(), vals[a:b], vout[a:b])
+            for a, b in zip(starts[:-1], starts[1:])]
+    plan = gms.BatchedMultisplit(segs)
+    assert plan.launches == 1
+    plan.run(use_graph=True)
+    torch.cuda.synchronize()
+    hk, hv, hko, hvo = host(keys), host(vals), host(kout), host(vout)
+    for i in range(0, len(sizes), 97):
+        a, b = starts[i], starts[i + 1]
+        rk, rv, _ = o.multisplit(hk[a:b], o.Desc(o.DELTA, 256), hv[a:b])
+        np.testing.assert_array_equal(hko[a:b], rk)
+        np.testing.assert_array_equal(hvo[a:b], rv)
+    plan.close()
