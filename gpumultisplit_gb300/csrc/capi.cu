@@ -273,25 +273,24 @@ gms_status compaction_impl(const uint32_t* kin, const uint32_t* vin, uint32_t* k
 // ------------------------------------------------ more than 256 buckets
 // B in (256, 65536] (RANGE: to GMS_RANGE_BIG_MAX splitters), 32-bit keys and
 // values, through the one-call entry points: two stable multisplits on the
-// digits of the bucket id, id & 255 into the scratch's ping-pong buffers, then
-// id >> 8 into the output.  Offsets come from a histogram of the whole ids.
-int big_high_logb(uint32_t B) {
-  const uint32_t hi = (B + 255u) / 256u;  // values of the high digit
-  int l = 1;
-  while ((1u << l) < hi) ++l;
-  return l;
-}
-
+// digits of the bucket id, the low half of its bits into the scratch's
+// ping-pong buffers, then the high half into the output.  Halving the bits
+// keeps both passes at a small bucket count (B = 1000: 32 x 32 buckets), which
+// is cheaper than a 256-bucket pass and a small one.  Offsets come from a
+// histogram of the whole ids.
 struct BigLayout {
-  int logb_hi;
-  size_t ms_bytes;  // scratch of either pass (with its bucket bytes)
+  int logb_lo, logb_hi;  // bits of the low and the high digit
+  size_t ms_bytes;       // scratch of either pass (with its bucket bytes)
   size_t off_keys, off_vals, off_hist, bytes;
 };
 
 BigLayout big_layout(uint32_t n, uint32_t B, bool kv) {
   BigLayout L;
-  L.logb_hi = big_high_logb(B);
-  const size_t a = make_geometry(n, 8, kv).bytes_full, b = make_geometry(n, L.logb_hi, kv).bytes_full;
+  int bits = 0;
+  while ((1u << bits) < B) ++bits;  // 9..16
+  L.logb_lo = (bits + 1) / 2;
+  L.logb_hi = bits - L.logb_lo;
+  const size_t a = make_geometry(n, L.logb_lo, kv).bytes_full, b = make_geometry(n, L.logb_hi, kv).bytes_full;
   L.ms_bytes = a > b ? a : b;
   L.off_keys = align_up(L.ms_bytes, 256);
   L.off_vals = align_up(L.off_keys + size_t(n) * 4, 256);
@@ -376,10 +375,10 @@ gms_status multisplit_big_impl(const uint32_t* kin, const uint32_t* vin, uint32_
     c.kout = pass == 0 ? tk : kout;
     c.vout = kv ? (pass == 0 ? tv : vout) : nullptr;
     c.n = n;
-    c.logb = pass == 0 ? 8 : L.logb_hi;
+    c.logb = pass == 0 ? L.logb_lo : L.logb_hi;
     c.kv = kv;
     c.bp.base = bp;
-    c.bp.digit_shift = pass == 0 ? 0u : 8u;
+    c.bp.digit_shift = pass == 0 ? 0u : uint32_t(L.logb_lo);
     c.scratch = base;
     c.bucket_bytes = base + make_geometry(n, c.logb, kv).off_buckets;
     c.stream = stream;

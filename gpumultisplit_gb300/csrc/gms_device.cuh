@@ -164,7 +164,7 @@ struct BucketParams {
   uint32_t num_buckets;       // B
 };
 
-// v modulo b (b in [2, 256]): a mask for powers of two, a division otherwise.
+// v modulo b (b >= 2): a mask for powers of two, a division otherwise.
 __device__ __forceinline__ uint32_t reduce_mod(uint32_t v, uint32_t b) {
   return (b & (b - 1)) == 0 ? (v & (b - 1)) : (v % b);
 }
@@ -417,8 +417,9 @@ struct DescPolicy64 {
 // ------------------------------------------- more than 256 buckets
 // B from 257 to 65536 (RANGE: to GMS_RANGE_BIG_MAX splitters) runs as two
 // stable multisplits on the digits of the bucket id, least significant first:
-// the low 8 bits, then id >> 8.  Stable passes make the result the
-// multisplit by the whole id.  DigitId returns digit (id >> shift) of the id.
+// the low half of its bits, then the rest.  Stable passes make the result the
+// multisplit by the whole id.  DigitId returns digit (id >> shift) of the id,
+// 2^LOGB values wide.
 #ifndef GMS_RANGE_BIG_MAX
 #define GMS_RANGE_BIG_MAX 8192
 #endif
@@ -426,7 +427,7 @@ constexpr uint32_t BIG_MAX_BUCKETS = 65536;
 
 struct BucketParamsBig {
   BucketParams base;     // base.num_buckets = B, the whole bucket count
-  uint32_t digit_shift;  // 0 for the low digit, 8 for the high one
+  uint32_t digit_shift;  // 0 for the low digit, its width for the high one
 };
 
 // Shared words of the full identifier: RANGE keeps up to GMS_RANGE_BIG_MAX

@@ -56,8 +56,8 @@ typedef enum gms_status {
  * gms_multisplit_key_only / _key_value, gms_multisplit_scratch_bytes and
  * gms_histogram also take B from 257 to 65536 (RANGE: up to 8192 splitters).
  * The multisplit then runs as two stable multisplits on the digits of the
- * bucket id (id & 255, then id >> 8), through buffers in the scratch; the
- * result is the same stable order.  The stage entry points, the batched and
+ * bucket id (the low half of its bits, then the high half), through buffers
+ * in the scratch; the result is the same stable order.  The stage entry points, the batched and
  * serving forms and the 64-bit entry points take B <= 256.
  *
  *  GMS_BUCKET_DELTA       key * B >> 32 (64-bit product): B equal-width key ranges.
