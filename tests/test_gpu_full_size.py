@@ -110,6 +110,35 @@ def test_kv_multisplit_beyond_2p31(gms_lib):
     assert offs == [int(x) for x in starts.cpu()]
 
 
+def test_u64_kv_multisplit_beyond_2p31(gms_lib):
+    """64-bit keys and values, n above 2^31: element offsets past 2^34 bytes and
+    32-bit positions near their top (buckets ascending, a stable permutation,
+    offsets equal to the bucket starts)."""
+    B = 256
+    n = (1 << 31) + 4099
+    kin = datagen.uniform_u64(n, 18, device="cuda")
+    vin = torch.arange(n, dtype=torch.int64, device="cuda")
+    kout, vout = torch.empty_like(kin), torch.empty_like(vin)
+    ctx = gms.multisplit_context(B)
+    gms.multisplit_wide_allocate(n, ctx, 8, 8)
+    offs = gms.multisplit_wide(kin, kout, n, ctx, gms.delta_bucket(), vin, vout, multisplit_offset=True)
+    torch.cuda.synchronize()
+    assert gms.read_device_error(ctx) == 0
+    del ctx, vin
+    seen = torch.zeros(n, dtype=torch.int8, device="cuda")
+    seen[vout] = 1
+    assert bool(seen.all()), "values are not a permutation of the indices"
+    del seen
+    assert torch.equal(kout, kin[vout]), "keys did not travel with their values"
+    del kin
+    b = (kout >> 56) & 0xFF  # delta on 64-bit keys at B = 256: the top 8 bits
+    assert bool((b[1:] >= b[:-1]).all()), "buckets not ascending"
+    assert bool((vout[1:] > vout[:-1])[b[1:] == b[:-1]].all()), "input order not kept inside a bucket"
+    counts = torch.bincount(b, minlength=B)
+    starts = torch.cumsum(counts, 0) - counts
+    assert offs == [int(x) for x in starts.cpu()]
+
+
 def test_batched_scan_groups_beyond_2p32(gms_lib):
     """A batch whose keys add up to more than 2^32 is scanned in groups; every
     segment keeps the multisplit properties (key-only: ascending buckets, and
