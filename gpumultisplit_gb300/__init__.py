@@ -44,7 +44,8 @@ from .api import (  # noqa: F401
     multisplit_sort_6bit, multisplit_sort_6bit_allocate, multisplit_sort_6bit_allocate_pairs, multisplit_sort_6bit_pairs,
     multisplit_sort_8bit, multisplit_sort_8bit_allocate, multisplit_sort_8bit_allocate_pairs, multisplit_sort_8bit_pairs,
     multisplit_sort_bits, multisplit_sort_bits_allocate, multisplit_sort_bits_pairs,
-    multisplit_sort_wide, multisplit_sort_wide_allocate, multisplit_wide, multisplit_wide_allocate,
+    multisplit_histogram_wide, multisplit_sort_wide, multisplit_sort_wide_allocate, multisplit_wide,
+    multisplit_wide_allocate,
 )
 from .batched import (  # noqa: F401
     BatchedMultisplit,

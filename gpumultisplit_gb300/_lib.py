@@ -96,6 +96,7 @@ _PROTOS = {
     "gms_sort_bits_key_value": [_P, _P, _P, _P, _U32, _I32, _I32, _I32, _P, _SZ, _P],
     "gms_multisplit_wide_scratch_bytes": [_U32, _U32, _I32, _I32, _PSZ],
     "gms_multisplit_wide": [_P, _P, _P, _P, _U32, _I32, _I32, _PDESC64, _P, _SZ, _PU32, _P],
+    "gms_histogram_wide": [_P, _U32, _I32, _PDESC64, _P, _P],
     "gms_sort_wide_scratch_bytes": [_U32, _I32, _I32, _I32, _I32, _I32, _PSZ],
     "gms_sort_wide": [_P, _P, _P, _P, _U32, _I32, _I32, _I32, _I32, _I32, _P, _SZ, _P],
     "gms_sort_7bit_scratch_bytes": [_U32, _I32, _PSZ],

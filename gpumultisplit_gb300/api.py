@@ -356,6 +356,16 @@ def multisplit_wide(d_key_in, d_key_out, num_elements: int, context: multisplit_
     return _export_offsets(offs, multisplit_offset)
 
 
+def multisplit_histogram_wide(d_key_in, num_elements: int, d_histogram, num_buckets: int,
+                              bucket_identifier: BucketIdentifier, stream=None) -> None:
+    """Adds per-bucket counts of 32- or 64-bit keys (int32 / int64 tensor) into
+    d_histogram[0..B) (int32, zeroed by the caller), B <= 256."""
+    kb = _elem_bytes(d_key_in)
+    desc = bucket_identifier.desc64(num_buckets)
+    check(_lib.load().gms_histogram_wide(_ptr(d_key_in, kb), num_elements, kb, ctypes.byref(desc),
+                                         _ptr(d_histogram), _stream(stream)), "multisplit_histogram_wide")
+
+
 def multisplit_sort_wide_allocate(n_elements: int, context, key_bytes: int, value_bytes: int = 0,
                                   begin_bit: int = 0, end_bit: int | None = None, digit_bits: int = 8) -> None:
     """Scratch for a stable sort of key_bytes-wide keys (with value_bytes-wide

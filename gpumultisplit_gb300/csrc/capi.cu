@@ -877,6 +877,36 @@ gms_status gms_multisplit_wide(const void* d_key_in, const void* d_value_in, voi
                       kv ? value_bytes / 4 : 1);
 }
 
+gms_status gms_histogram_wide(const void* d_key_in, uint32_t n, int key_bytes, const gms_bucket_desc64* desc,
+                              int32_t* d_hist, gms_stream_t stream) {
+  if (key_bytes == 4) {
+    gms_bucket_desc d32;
+    gms_status st = narrow_desc(desc, &d32);
+    if (st != GMS_SUCCESS) return st;
+    return gms_histogram(static_cast<const uint32_t*>(d_key_in), n, &d32, d_hist, stream);
+  }
+  if (key_bytes != 8) return GMS_ERROR_INVALID_VALUE;
+  int logb = 0;
+  gms_status st = check_desc64(desc, &logb);
+  if (st != GMS_SUCCESS) return st;
+  if (d_hist == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (n == 0) return GMS_SUCCESS;
+  if (d_key_in == nullptr || (reinterpret_cast<uintptr_t>(d_key_in) & 7u) != 0) return GMS_ERROR_INVALID_VALUE;
+  const auto* keys = static_cast<const uint64_t*>(d_key_in);
+  const BucketParams64 bp = to_params64(desc);
+  cudaError_t e = cudaErrorInvalidValue;
+  switch (desc->kind) {
+    case KIND_DELTA: e = run_histogram64<KIND_DELTA>(keys, n, logb, bp, d_hist, stream); break;
+    case KIND_DIV: e = run_histogram64<KIND_DIV>(keys, n, logb, bp, d_hist, stream); break;
+    case KIND_BITS: e = run_histogram64<KIND_BITS>(keys, n, logb, bp, d_hist, stream); break;
+    case KIND_RANGE: e = run_histogram64<KIND_RANGE>(keys, n, logb, bp, d_hist, stream); break;
+    case KIND_MASK: e = run_histogram64<KIND_MASK>(keys, n, logb, bp, d_hist, stream); break;
+    case KIND_EVEN_FLOAT: e = run_histogram64<KIND_EVEN_FLOAT>(keys, n, logb, bp, d_hist, stream); break;
+    default: break;
+  }
+  return cuda_status(e);
+}
+
 gms_status gms_sort_wide_scratch_bytes(uint32_t max_elements, int key_bytes, int value_bytes, int begin_bit,
                                        int end_bit, int digit_bits, size_t* bytes) {
   SortSchedule sch;

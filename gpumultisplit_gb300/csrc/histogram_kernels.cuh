@@ -35,6 +35,43 @@ __global__ void __launch_bounds__(HIST_THREADS) histogram_kernel(const uint32_t*
   if (threadIdx.x < num_bins && total) atomicAdd(&hist[threadIdx.x], int32_t(total));
 }
 
+// Histogram of 64-bit keys (the 64-bit identifiers, B <= 256): the same
+// persistent counting as histogram_kernel, the keys read as 16-byte vectors of
+// two when the array is 16-byte aligned.
+template <int LOGB, int KIND>
+__global__ void __launch_bounds__(HIST_THREADS) histogram64_kernel(const uint64_t* __restrict__ keys, uint32_t n,
+                                                                   int32_t* __restrict__ hist, BucketParams64 bp,
+                                                                   uint32_t num_bins) {
+  using P = DescPolicy64<KIND, LOGB>;
+  using Counter = KeyCounter<LOGB, typename P::Id>;
+  __shared__ uint32_t s_hist[Counter::smem_words(HIST_WARPS)];
+  __shared__ __align__(16) uint32_t s_split[P::SMEM_WORDS];
+  P::prepare(s_split, bp);
+  Counter counter(P::make(bp, s_split), s_hist);
+  counter.clear_shared();
+  __syncthreads();
+  const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0;
+  for (uint32_t base = blockIdx.x * HIST_CHUNK; base < n; base += gridDim.x * HIST_CHUNK) {
+    if (vec && n - base >= HIST_CHUNK) {
+#pragma unroll 4
+      for (int k = 0; k < HIST_IPT / 2; ++k) {
+        const uint4 q = ld_nc_v4(reinterpret_cast<const uint32_t*>(keys + base + (uint32_t(k) * HIST_THREADS + threadIdx.x) * 2u));
+        counter.template add_bucket<0>(counter.ident(uint64_t(q.x) | (uint64_t(q.y) << 32)), true);
+        counter.template add_bucket<1>(counter.ident(uint64_t(q.z) | (uint64_t(q.w) << 32)), true);
+      }
+    } else {
+#pragma unroll 4
+      for (int k = 0; k < HIST_IPT; ++k) {
+        const uint32_t i = base + uint32_t(k) * HIST_THREADS + threadIdx.x;
+        const bool valid = i < n;
+        counter.add_bucket(counter.ident(valid ? keys[i] : 0ull), valid);
+      }
+    }
+  }
+  const uint32_t total = counter.block_total();
+  if (threadIdx.x < num_bins && total) atomicAdd(&hist[threadIdx.x], int32_t(total));
+}
+
 // Histogram over B > 256 bins (to 65536): the whole bucket id of every key
 // (big_bucket_id) added with one global atomic per key into hist[0..B).
 // Persistent grid, strided over keys.

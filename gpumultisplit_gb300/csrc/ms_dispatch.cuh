@@ -216,6 +216,34 @@ cudaError_t run_multisplit_wide_l(const MsCallWide& c, int stages) {
   return cudaErrorInvalidValue;  // 32-bit keys and values take run_multisplit
 }
 
+template <int KIND, int LOGB>
+cudaError_t run_histogram64_t(const uint64_t* keys, uint32_t n, const BucketParams64& bp, int32_t* hist,
+                              cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  static std::atomic<int> per_sm{0};
+  auto kern = histogram64_kernel<LOGB, KIND>;
+  const uint32_t grid = persistent_grid(kern, HIST_THREADS, uint32_t((uint64_t(n) + HIST_CHUNK - 1) / HIST_CHUNK),
+                                        per_sm);
+  kern<<<grid, HIST_THREADS, 0, stream>>>(keys, n, hist, bp, bp.num_buckets);
+  return cudaGetLastError();
+}
+
+template <int KIND>
+cudaError_t run_histogram64(const uint64_t* keys, uint32_t n, int logb, const BucketParams64& bp, int32_t* hist,
+                            cudaStream_t stream) {
+  switch (logb) {
+    case 1: return run_histogram64_t<KIND, 1>(keys, n, bp, hist, stream);
+    case 2: return run_histogram64_t<KIND, 2>(keys, n, bp, hist, stream);
+    case 3: return run_histogram64_t<KIND, 3>(keys, n, bp, hist, stream);
+    case 4: return run_histogram64_t<KIND, 4>(keys, n, bp, hist, stream);
+    case 5: return run_histogram64_t<KIND, 5>(keys, n, bp, hist, stream);
+    case 6: return run_histogram64_t<KIND, 6>(keys, n, bp, hist, stream);
+    case 7: return run_histogram64_t<KIND, 7>(keys, n, bp, hist, stream);
+    case 8: return run_histogram64_t<KIND, 8>(keys, n, bp, hist, stream);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 template <int KIND>
 cudaError_t run_multisplit_wide(const MsCallWide& c, int stages) {
   switch (c.logb) {
@@ -416,7 +444,10 @@ cudaError_t run_big_histogram(const uint32_t* keys, uint32_t n, const BucketPara
   template cudaError_t gms::run_big_histogram<K>(const uint32_t*, uint32_t, const gms::BucketParams&, uint32_t*, \
                                                  cudaStream_t);
 
-#define GMS_INSTANTIATE_WIDE(K) template cudaError_t gms::run_multisplit_wide<K>(const gms::MsCallWide&, int);
+#define GMS_INSTANTIATE_WIDE(K)                                                                          \
+  template cudaError_t gms::run_multisplit_wide<K>(const gms::MsCallWide&, int);                        \
+  template cudaError_t gms::run_histogram64<K>(const uint64_t*, uint32_t, int, const gms::BucketParams64&, \
+                                               int32_t*, cudaStream_t);
 
 #define GMS_INSTANTIATE_BATCH_WARP(K) template cudaError_t gms::run_batch_warp<K>(const gms::BatchClassLaunch&);
 

@@ -159,6 +159,10 @@ struct MsCallWide {
 // Defined per identifier kind in inst_wide.cu (compiled once per kind).
 template <int KIND>
 cudaError_t run_multisplit_wide(const MsCallWide& c, int stages);
+// Histogram of 64-bit keys into hist[0..B) (inst_wide.cu).
+template <int KIND>
+cudaError_t run_histogram64(const uint64_t* keys, uint32_t n, int logb, const BucketParams64& bp, int32_t* hist,
+                            cudaStream_t stream);
 
 // One digit pass of a multisplit with more than 256 buckets (32-bit keys and
 // values): 2^logb buckets of digit (id >> bp.digit_shift); the scratch is laid

@@ -240,6 +240,10 @@ gms_status gms_multisplit_wide_scratch_bytes(uint32_t max_elements, uint32_t num
 gms_status gms_multisplit_wide(const void* d_key_in, const void* d_value_in, void* d_key_out, void* d_value_out,
                                uint32_t n, int key_bytes, int value_bytes, const gms_bucket_desc64* desc,
                                void* d_scratch, size_t scratch_bytes, uint32_t* h_offsets, gms_stream_t stream);
+/* Adds the count of every bucket into the caller-zeroed d_hist[0..B), B <= 256
+ * (as gms_histogram; 4-byte keys take gms_histogram itself). */
+gms_status gms_histogram_wide(const void* d_key_in, uint32_t n, int key_bytes, const gms_bucket_desc64* desc,
+                              int32_t* d_hist, gms_stream_t stream);
 /* Stable sort by key bits [begin_bit, end_bit), end_bit <= 8 * key_bytes, in
  * digits of digit_bits (4..8) bits, least significant first. */
 gms_status gms_sort_wide_scratch_bytes(uint32_t max_elements, int key_bytes, int value_bytes, int begin_bit,

@@ -277,6 +277,14 @@ def multisplit64(keys, d: Desc64, values=None):
     return kout, vout, offs
 
 
+def histogram64(keys, d: Desc64) -> np.ndarray:
+    keys = _u64(keys)
+    hist = np.zeros(d.num_buckets, np.int32)
+    cd = d.c()
+    lib().oracle_histogram64(_p(keys), ctypes.c_uint32(keys.size), ctypes.byref(cd), _p(hist))
+    return hist
+
+
 def sort_bits64(keys, values=None, begin_bit: int = 0, end_bit: int = 64, digit_bits: int = 8):
     """Stable sort of 64-bit keys by bits [begin_bit, end_bit) in digit_bits-wide passes."""
     keys = _u64(keys)

@@ -387,3 +387,8 @@ int oracle_sort_bits64(const uint64_t* kin, uint64_t* kout, const void* vin, voi
   }
   return 0;
 }
+
+/* Adds the per-bucket counts of 64-bit keys into hist (as oracle_histogram). */
+void oracle_histogram64(const uint64_t* kin, uint32_t n, const oracle_desc64* d, int32_t* hist) {
+  for (uint32_t i = 0; i < n; ++i) hist[oracle_bucket64(d, kin[i])]++;
+}

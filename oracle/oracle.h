@@ -61,6 +61,7 @@ typedef struct oracle_desc64 {
 uint32_t oracle_bucket64(const oracle_desc64* d, uint64_t key);
 void oracle_multisplit64(const uint64_t* kin, uint64_t* kout, const void* vin, void* vout, int value_bytes,
                          uint32_t n, const oracle_desc64* d, uint32_t* offsets);
+void oracle_histogram64(const uint64_t* kin, uint32_t n, const oracle_desc64* d, int32_t* hist);
 int oracle_sort_bits64(const uint64_t* kin, uint64_t* kout, const void* vin, void* vout, int value_bytes, uint32_t n,
                        uint64_t* tmp_k, void* tmp_v, int begin_bit, int end_bit, int digit_bits);
 

@@ -228,3 +228,34 @@ def test_wide_checks_alignment_on_device_buffers(gms_lib):
                                  ctypes.byref(d), ctx.d_temp_storage.data_ptr(), ctx.temp_storage_bytes, None,
                                  torch.cuda.current_stream().cuda_stream)
     assert st == gms._lib.GMS_ERROR_INVALID_VALUE
+
+
+@pytest.mark.parametrize("B", [7, 32, 256])
+@pytest.mark.parametrize("kind", [0, 1, 2, 3, 4, 5], ids=lambda k: KIND_NAMES[k])
+def test_u64_histogram(gms_lib, oracle_mod, B, kind):
+    """Histogram of 64-bit keys: B bins, the words after them untouched; an
+    array 8- but not 16-byte aligned takes the element loads."""
+    o = oracle_mod
+    if kind == o.BITS and B & (B - 1):
+        pytest.skip("bit-field buckets are powers of two")
+    ident, d, keep = identifiers64(o, kind, B, seed=B)
+    n = 300007
+    keys = datagen.as_u64(datagen.uniform_u64(n, 70 + B + kind))
+    want = o.histogram64(keys, d)
+    for pad in (0, 1):
+        buf = torch.full((B + 64,), -7, dtype=torch.int32, device="cuda")
+        buf[:B].zero_()
+        gms.multisplit_histogram_wide(dev64(keys, pad), n, buf[:B], B, ident)
+        got = buf.cpu().numpy()
+        np.testing.assert_array_equal(got[:B], want)
+        assert (got[B:] == -7).all()
+    del keep
+
+
+def test_histogram_wide_32bit_keys_is_the_plain_histogram(gms_lib, oracle_mod):
+    o = oracle_mod
+    n, B = 100003, 100
+    keys = datagen.as_u32(datagen.uniform_u32(n, 5))
+    h = torch.zeros(B, dtype=torch.int32, device="cuda")
+    gms.multisplit_histogram_wide(to_dev(keys), n, h, B, gms.delta_bucket())
+    np.testing.assert_array_equal(h.cpu().numpy(), o.histogram(keys, o.Desc(o.DELTA, B)))

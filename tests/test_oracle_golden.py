@@ -204,6 +204,8 @@ def test_oracle_64bit_keys_against_numpy(oracle_mod):
             assert np.array_equal(offs, np.searchsorted(np.sort(ids), np.arange(B)).astype(np.uint32))
         f = o.buckets64(keys, o.Desc64(o.EVEN_FLOAT, B, lower=2**40, inverse_delta=B / 2**64))
         assert f.max() < B
+        assert np.array_equal(o.histogram64(keys, o.Desc64(o.DELTA, B)),
+                              np.bincount(cases[0][1].astype(np.int64), minlength=B).astype(np.int32))
     ks, vs = o.sort_bits64(keys, vals, 0, 64, 8)
     assert np.array_equal(ks, np.sort(keys)) and np.array_equal(vs, vals[np.argsort(keys, kind="stable")])
     ks, vs = o.sort_bits64(keys, vals.astype(np.uint32), 13, 47, 7)
