@@ -6,7 +6,7 @@ its sources first):  python tests/golden/make_golden.py
 Every case records its inputs by generator + seed (gpumultisplit_gb300.datagen,
 a counter-based splitmix64 generator) together with the SHA-256 of the input,
 and the reference's outputs: full arrays for tiny cases, SHA-256 digests plus
-bucket offsets for the rest.  Outputs come from cpu_multisplit_general /
+bucket offsets for the rest (a digest of the offsets above 256 buckets).  Outputs come from cpu_multisplit_general /
 cpu_multisplit_pairs_general (src/cpu_functions.h:155-288) compiled from the
 reference sources, driven either by reference-style functors (key*B>>32 as top
 bits, delta_func's key/delta, ms_bucket_sort's bit field) or by the oracle's
@@ -66,7 +66,10 @@ def record(case: dict, keys: np.ndarray, kout: np.ndarray, vout, offsets) -> dic
         if vout is not None:
             case["values_out"] = [int(x) for x in vout]
     if offsets is not None:
-        case["offsets"] = offsets
+        if len(offsets) > 256:  # above 256 buckets: a digest of the offsets keeps the file small
+            case["offsets_sha256"] = sha(np.array(offsets, dtype=np.uint32))
+        else:
+            case["offsets"] = offsets
     return case
 
 
@@ -133,6 +136,20 @@ def main() -> None:
          "buckets": 256, "lower": 0, "inverse_delta": 2.0 ** -24, "values": True},
         {"name": "even_float_b32_keys", "dist": "uniform", "n": 5000, "seed": 17, "kind": oracle.EVEN_FLOAT,
          "buckets": 32, "lower": 1000, "inverse_delta": 32.0 / 4294967296.0, "values": False},
+        # Bucket counts the reference's GPU API does not take (powers of two to 256
+        # only); its CPU multisplit takes any count, so the order is still its own.
+        {"name": "delta_b12_pairs", "dist": "uniform", "n": 30011, "seed": 41, "kind": oracle.DELTA, "buckets": 12,
+         "values": True},
+        {"name": "div_b5_keys", "dist": "uniform", "n": 7777, "seed": 42, "kind": oracle.DIV, "buckets": 5,
+         "param": 100003, "values": False},
+        {"name": "range_b100_pairs_zipf", "dist": "zipf", "n": 20001, "seed": 43, "kind": oracle.RANGE,
+         "buckets": 100, "splitter_seed": 44, "values": True},
+        {"name": "delta_b1000_pairs", "dist": "uniform", "n": 50001, "seed": 45, "kind": oracle.DELTA,
+         "buckets": 1000, "values": True},
+        {"name": "range_b4096_pairs", "dist": "uniform", "n": 60000, "seed": 46, "kind": oracle.RANGE,
+         "buckets": 4096, "splitter_seed": 47, "values": True},
+        {"name": "delta_b65536_keys", "dist": "uniform", "n": 100000, "seed": 48, "kind": oracle.DELTA,
+         "buckets": 65536, "values": False},
     ]
     for case in desc_cases:
         case = dict(case, op="multisplit")

@@ -50,6 +50,8 @@ def test_oracle_matches_golden(golden, oracle_mod):
             ko, vo, offs = o.multisplit(keys, desc_of(o, case), vals)
             if "offsets" in case:
                 assert [int(x) for x in offs] == case["offsets"], case["name"]
+            if "offsets_sha256" in case:
+                assert sha(np.asarray(offs, dtype=np.uint32)) == case["offsets_sha256"], case["name"]
         elif case["op"] == "compaction":
             ko, vo, n0 = o.compaction(keys, desc_of(o, case), vals)
             assert n0 == case["num_bucket0"], case["name"]
