@@ -318,3 +318,30 @@ def test_batch_plan_classes_follow_the_table(gms_lib):
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(ImportError):
         _lib.load(tmp_path / "libgpumultisplit.so")
+
+
+def test_big_bucket_scratch_layout(gms_lib):
+    """Above 256 buckets the scratch holds the larger digit pass's scratch (with
+    its bucket bytes), ping-pong keys (and values) and a B-word histogram; the
+    id's bits are split in half between the passes."""
+    def nbytes(n, B, kv):
+        out = ctypes.c_size_t()
+        assert gms_lib.gms_multisplit_scratch_bytes(n, B, kv, ctypes.byref(out)) == 0
+        return out.value
+
+    def align(x):
+        return (x + 255) // 256 * 256
+
+    def full(n, logb):  # one multisplit's scratch with bucket bytes, 4096-key tiles
+        tiles = (n + 4095) // 4096
+        m = (1 << logb) * tiles
+        return align(align(align(256 + 4 * m) + 8 * ((m + 4095) // 4096)) + n)
+
+    for n in (1, 4096, 1000003):
+        for B in (257, 1000, 4096, 65536):
+            bits = (B - 1).bit_length()
+            lo, hi = (bits + 1) // 2, bits - (bits + 1) // 2
+            ms = max(full(n, lo), full(n, hi))
+            keys_end = align(ms) + 4 * n
+            assert nbytes(n, B, 0) == align(align(keys_end) + 4 * B)
+            assert nbytes(n, B, 1) == align(align(align(keys_end) + 4 * n) + 4 * B)
