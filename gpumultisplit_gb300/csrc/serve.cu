@@ -22,6 +22,8 @@ namespace {
 
 constexpr size_t kAlign = 256;
 constexpr int kSlots = 2;  // streams, and rounds in flight at most
+constexpr size_t kInitialStaging = size_t(8) << 20;  // pinned bytes per slot for round tables
+constexpr size_t kInitialReadback = size_t(64) << 10;  // pinned bytes per slot for read-back words
 
 // First-fit allocator over [0, size) with coalescing free blocks.
 class Arena {
@@ -459,6 +461,14 @@ gms_status gms_server_create(void* d_arena, size_t arena_bytes, gms_server_t* se
       delete s;
       return GMS_ERROR_CUDA;
     }
+  }
+  // Pinned staging for the round tables and the read-back words, allocated
+  // up front: growing them later frees pinned memory, which waits for the
+  // whole device and stalls the round in flight on the other stream.  A
+  // failure here only leaves the growth to the first rounds.
+  for (int i = 0; i < kSlots; ++i) {
+    ensure_pinned(&s->pinned[i], &s->pinned_cap[i], kInitialStaging);
+    ensure_pinned(reinterpret_cast<void**>(&s->readback[i]), &s->readback_cap[i], kInitialReadback);
   }
   s->worker = std::thread(scheduler, s);
   *server = s;
