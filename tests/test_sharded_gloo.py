@@ -55,7 +55,7 @@ def _worker(rank, port, n, cut, B, kind, out_dir):
 
 
 @pytest.mark.parametrize("n,cut,B,kind", [(100003, 40000, 256, 0), (50000, 50000, 32, 3), (30001, 0, 8, 0),
-                                          (4097, 4097, 2, 3)])
+                                          (4097, 4097, 2, 3), (60001, 25000, 1000, 0), (40000, 10000, 12, 3)])
 def test_sharded_offsets_reproduce_single_multisplit(oracle_mod, tmp_path, n, cut, B, kind):
     mp.start_processes(_worker, args=(_free_port(), n, cut, B, kind, str(tmp_path)), nprocs=WORLD,
                        start_method="spawn", join=True)
