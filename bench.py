@@ -570,6 +570,12 @@ def sweep_big(n, dev, timed, emit, cpu_rate, sample):
         emit(f"multisplit kv B={B} uniform {ident_name} (two digit passes)", ms, 20, "pass" if ok else "FAIL",
              cpu_rate(lambda: oracle.multisplit(hk, desc, hv), 1))
         gms.multisplit_release_memory(ctx)
+        hist = torch.zeros(B, dtype=torch.int32, device=dev)
+        ms = timed(lambda: gms.multisplit_histogram(kin, n, hist, B, ident))
+        hist.zero_()
+        gms.multisplit_histogram(kin, n, hist, B, ident)
+        emit(f"histogram {B} bins uniform {ident_name}", ms, 4, "pass" if int(hist.sum()) == n else "FAIL",
+             cpu_rate(lambda: oracle.histogram(hk, desc), 1))
 
 def run_tiny_segments(dev, count: int = 200000, seed: int = 9):
     """Many small multisplits: `count` key-value segments of 1..512 keys (uniform

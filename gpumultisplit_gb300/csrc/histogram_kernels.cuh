@@ -73,17 +73,49 @@ __global__ void __launch_bounds__(HIST_THREADS) histogram64_kernel(const uint64_
 }
 
 // Histogram over B > 256 bins (to 65536): the whole bucket id of every key
-// (big_bucket_id) added with one global atomic per key into hist[0..B).
-// Persistent grid, strided over keys.
-template <int KIND>
+// (big_bucket_id).  Up to BIG_HIST_SMEM_BINS bins every block counts into a
+// shared histogram (dynamic shared memory) and adds its non-zero bins into
+// hist[0..B) at the end; above that, one global atomic per key.  Persistent
+// grid, strided over keys.
+constexpr uint32_t BIG_HIST_SMEM_BINS = 8192;
+
+template <int KIND, bool SHARED>
 __global__ void __launch_bounds__(HIST_THREADS) big_histogram_kernel(const uint32_t* __restrict__ keys, uint32_t n,
                                                                      BucketParams p, uint32_t* __restrict__ hist) {
   __shared__ uint32_t s_split[big_identifier_smem_words<KIND>()];
+  extern __shared__ uint32_t s_bins[];  // SHARED: B counters
+  const uint32_t B = p.num_buckets;
+  if constexpr (SHARED) {
+    for (uint32_t b = threadIdx.x; b < B; b += HIST_THREADS) s_bins[b] = 0u;
+  }
   prepare_big_identifier<KIND>(s_split, p);
   __syncthreads();
+  auto add = [&](uint32_t key) {
+    const uint32_t b = big_bucket_id<KIND>(key, p, s_split);
+    if constexpr (SHARED)
+      atomicAdd(&s_bins[b], 1u);
+    else
+      atomicAdd(&hist[b], 1u);
+  };
+  // 16-byte vectors of four keys while whole vectors remain (keys 16-byte
+  // aligned), then single keys.
   const uint32_t stride = gridDim.x * HIST_THREADS;
-  for (uint32_t i = blockIdx.x * HIST_THREADS + threadIdx.x; i < n; i += stride)
-    atomicAdd(&hist[big_bucket_id<KIND>(keys[i], p, s_split)], 1u);
+  const uint32_t nv = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0 ? n / 4 : 0u;
+  for (uint32_t v = blockIdx.x * HIST_THREADS + threadIdx.x; v < nv; v += stride) {
+    const uint4 q = ld_nc_v4(keys + 4 * v);
+    add(q.x);
+    add(q.y);
+    add(q.z);
+    add(q.w);
+  }
+  for (uint32_t i = 4 * nv + blockIdx.x * HIST_THREADS + threadIdx.x; i < n; i += stride) add(keys[i]);
+  if constexpr (SHARED) {
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < B; b += HIST_THREADS) {
+      const uint32_t c = s_bins[b];
+      if (c) atomicAdd(&hist[b], c);
+    }
+  }
 }
 
 }  // namespace gms

@@ -13,10 +13,12 @@
 
 namespace gms {
 
-// Raise a kernel's dynamic shared-memory limit once per device (bit per device id).
+// Raise a kernel's dynamic shared-memory limit to `bytes` once per device (bit
+// per device id); needed once its static plus dynamic shared memory passes 48 KB.
 template <class Kernel>
-inline cudaError_t ensure_smem_limit(Kernel k, size_t bytes, std::atomic<uint64_t>& done_mask) {
-  if (bytes <= 48 * 1024) return cudaSuccess;
+inline cudaError_t ensure_smem_limit(Kernel k, size_t bytes, std::atomic<uint64_t>& done_mask,
+                                     size_t static_bytes = 0) {
+  if (bytes + static_bytes <= 48 * 1024) return cudaSuccess;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
@@ -424,10 +426,23 @@ template <int KIND>
 cudaError_t run_big_histogram(const uint32_t* keys, uint32_t n, const BucketParams& p, uint32_t* hist,
                               cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
+  const uint32_t work = uint32_t((uint64_t(n) / 4 + HIST_THREADS) / HIST_THREADS);  // blocks of 4-key vectors
+  if (p.num_buckets <= BIG_HIST_SMEM_BINS) {
+    // Per-block shared histograms; the limit and the occupancy query assume the largest size.
+    static std::atomic<int> per_sm{0};
+    static std::atomic<uint64_t> smem_done{0};
+    auto kern = big_histogram_kernel<KIND, true>;
+    const size_t smem = size_t(p.num_buckets) * 4;
+    cudaError_t e = ensure_smem_limit(kern, size_t(BIG_HIST_SMEM_BINS) * 4, smem_done,
+                                      size_t(big_identifier_smem_words<KIND>()) * 4);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid = persistent_grid(kern, HIST_THREADS, work, per_sm, size_t(BIG_HIST_SMEM_BINS) * 4);
+    kern<<<grid, HIST_THREADS, smem, stream>>>(keys, n, p, hist);
+    return cudaGetLastError();
+  }
   static std::atomic<int> per_sm{0};
-  auto kern = big_histogram_kernel<KIND>;
-  const uint32_t grid = persistent_grid(kern, HIST_THREADS, uint32_t((uint64_t(n) + HIST_THREADS - 1) / HIST_THREADS),
-                                        per_sm);
+  auto kern = big_histogram_kernel<KIND, false>;
+  const uint32_t grid = persistent_grid(kern, HIST_THREADS, work, per_sm);
   kern<<<grid, HIST_THREADS, 0, stream>>>(keys, n, p, hist);
   return cudaGetLastError();
 }
