@@ -276,12 +276,12 @@ gms_status compaction_impl(const uint32_t* kin, const uint32_t* vin, uint32_t* k
 // digits of the bucket id, the low half of its bits into the scratch's
 // ping-pong buffers, then the high half into the output.  Halving the bits
 // keeps both passes at a small bucket count (B = 1000: 32 x 32 buckets), which
-// is cheaper than a 256-bucket pass and a small one.  Offsets come from a
-// histogram of the whole ids.
+// is cheaper than a 256-bucket pass and a small one.  Offsets are read off the
+// output, which is sorted by the whole id.
 struct BigLayout {
   int logb_lo, logb_hi;  // bits of the low and the high digit
   size_t ms_bytes;       // scratch of either pass (with its bucket bytes)
-  size_t off_keys, off_vals, off_hist, bytes;
+  size_t off_keys, off_vals, off_hist, bytes;  // off_hist: B words for the bucket starts
 };
 
 BigLayout big_layout(uint32_t n, uint32_t B, bool kv) {
@@ -330,6 +330,19 @@ cudaError_t dispatch_digit_prescan(int kind, const DigitPass& c) {
     case KIND_RANGE: return run_digit_prescan_scan<KIND_RANGE>(c);
     case KIND_MASK: return run_digit_prescan_scan<KIND_MASK>(c);
     case KIND_EVEN_FLOAT: return run_digit_prescan_scan<KIND_EVEN_FLOAT>(c);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t dispatch_big_offsets(int kind, const uint32_t* sorted_keys, uint32_t n, const BucketParams& p,
+                                 uint32_t* starts, cudaStream_t s) {
+  switch (kind) {
+    case KIND_DELTA: return run_big_offsets<KIND_DELTA>(sorted_keys, n, p, starts, s);
+    case KIND_DIV: return run_big_offsets<KIND_DIV>(sorted_keys, n, p, starts, s);
+    case KIND_BITS: return run_big_offsets<KIND_BITS>(sorted_keys, n, p, starts, s);
+    case KIND_RANGE: return run_big_offsets<KIND_RANGE>(sorted_keys, n, p, starts, s);
+    case KIND_MASK: return run_big_offsets<KIND_MASK>(sorted_keys, n, p, starts, s);
+    case KIND_EVEN_FLOAT: return run_big_offsets<KIND_EVEN_FLOAT>(sorted_keys, n, p, starts, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -387,19 +400,12 @@ gms_status multisplit_big_impl(const uint32_t* kin, const uint32_t* vin, uint32_
     if (e != cudaSuccess) return cuda_status(e);
   }
   if (h_offsets == nullptr) return GMS_SUCCESS;
-  auto* hist = reinterpret_cast<uint32_t*>(base + L.off_hist);
-  cudaError_t e = cudaMemsetAsync(hist, 0, size_t(B) * 4, stream);
-  if (e == cudaSuccess) e = dispatch_big_histogram(desc->kind, kin, n, bp, hist, stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h_offsets, hist, size_t(B) * 4, cudaMemcpyDeviceToHost, stream);
+  // The output is sorted by the whole id: every bucket start is read off it.
+  auto* starts = reinterpret_cast<uint32_t*>(base + L.off_hist);
+  cudaError_t e = dispatch_big_offsets(desc->kind, kout, n, bp, starts, stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_offsets, starts, size_t(B) * 4, cudaMemcpyDeviceToHost, stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-  if (e != cudaSuccess) return cuda_status(e);
-  uint32_t run = 0;
-  for (uint32_t b = 0; b < B; ++b) {
-    const uint32_t c = h_offsets[b];
-    h_offsets[b] = run;
-    run += c;
-  }
-  return GMS_SUCCESS;
+  return cuda_status(e);
 }
 
 // ------------------------------------------------ 64-bit keys and values

@@ -118,4 +118,26 @@ __global__ void __launch_bounds__(HIST_THREADS) big_histogram_kernel(const uint3
   }
 }
 
+// Bucket starts of a multisplit by the whole bucket id, read off its output
+// (keys sorted by id, stably): key i starts every bucket b with
+// id(key[i-1]) < b <= id(key[i]) (key -1 reading as id -1), and buckets past
+// the last key's id start at n.  Every start is written exactly once.
+template <int KIND>
+__global__ void __launch_bounds__(HIST_THREADS) big_offsets_kernel(const uint32_t* __restrict__ sorted_keys,
+                                                                   uint32_t n, BucketParams p,
+                                                                   uint32_t* __restrict__ starts) {
+  __shared__ uint32_t s_split[big_identifier_smem_words<KIND>()];
+  prepare_big_identifier<KIND>(s_split, p);
+  __syncthreads();
+  const uint32_t B = p.num_buckets;
+  const uint32_t stride = gridDim.x * HIST_THREADS;
+  for (uint32_t i = blockIdx.x * HIST_THREADS + threadIdx.x; i < n; i += stride) {
+    const uint32_t cur = big_bucket_id<KIND>(sorted_keys[i], p, s_split);
+    const uint32_t first = i == 0 ? 0u : big_bucket_id<KIND>(sorted_keys[i - 1], p, s_split) + 1u;
+    for (uint32_t b = first; b <= cur; ++b) starts[b] = i;
+    if (i == n - 1)
+      for (uint32_t b = cur + 1; b < B; ++b) starts[b] = n;
+  }
+}
+
 }  // namespace gms

@@ -447,6 +447,18 @@ cudaError_t run_big_histogram(const uint32_t* keys, uint32_t n, const BucketPara
   return cudaGetLastError();
 }
 
+template <int KIND>
+cudaError_t run_big_offsets(const uint32_t* sorted_keys, uint32_t n, const BucketParams& p, uint32_t* starts,
+                            cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  static std::atomic<int> per_sm{0};
+  auto kern = big_offsets_kernel<KIND>;
+  const uint32_t grid = persistent_grid(kern, HIST_THREADS, uint32_t((uint64_t(n) + HIST_THREADS - 1) / HIST_THREADS),
+                                        per_sm);
+  kern<<<grid, HIST_THREADS, 0, stream>>>(sorted_keys, n, p, starts);
+  return cudaGetLastError();
+}
+
 }  // namespace gms
 
 #define GMS_INSTANTIATE_KIND(K)                                                                        \
@@ -457,7 +469,9 @@ cudaError_t run_big_histogram(const uint32_t* keys, uint32_t n, const BucketPara
 #define GMS_INSTANTIATE_BIG(K)                                                           \
   template cudaError_t gms::run_digit_prescan_scan<K>(const gms::DigitPass&);           \
   template cudaError_t gms::run_big_histogram<K>(const uint32_t*, uint32_t, const gms::BucketParams&, uint32_t*, \
-                                                 cudaStream_t);
+                                                 cudaStream_t);                                                 \
+  template cudaError_t gms::run_big_offsets<K>(const uint32_t*, uint32_t, const gms::BucketParams&, uint32_t*, \
+                                               cudaStream_t);
 
 #define GMS_INSTANTIATE_WIDE(K)                                                                          \
   template cudaError_t gms::run_multisplit_wide<K>(const gms::MsCallWide&, int);                        \

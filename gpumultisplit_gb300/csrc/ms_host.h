@@ -192,6 +192,11 @@ cudaError_t run_digit_postscan(const DigitPass& c);
 template <int KIND>
 cudaError_t run_big_histogram(const uint32_t* keys, uint32_t n, const BucketParams& p, uint32_t* hist,
                               cudaStream_t stream);
+// Bucket starts of a multisplit by the whole id, from its sorted output
+// (inst_big.cu): starts[0..p.num_buckets).
+template <int KIND>
+cudaError_t run_big_offsets(const uint32_t* sorted_keys, uint32_t n, const BucketParams& p, uint32_t* starts,
+                            cudaStream_t stream);
 
 // Histogram of keys[0..n) into hist[0..2^logb), accumulated with atomics.
 template <int KIND>
