@@ -1,5 +1,6 @@
 // Kernel instances of the digit passes (more than 256 buckets) for one
-// identifier kind: the prescans and the whole-id histogram.  The build compiles
+// identifier kind: the prescans, the whole-id histogram and the bucket starts
+// read off the sorted output.  The build compiles
 // this file once per kind with -DGMS_INST_KIND=<kind>.
 #include "ms_dispatch.cuh"
 
