@@ -285,7 +285,9 @@ def multisplit_key_value(d_key_in, d_value_in, d_key_out, d_value_out, num_eleme
 def _export_offsets(offs, target):
     if offs is None:
         return None
-    vals = list(offs)
+    import numpy as np
+
+    vals = np.ctypeslib.as_array(offs).tolist()  # far faster than list() on a ctypes array of 64 Ki entries
     if isinstance(target, list):
         target[:] = vals
     return vals
