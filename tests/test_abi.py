@@ -308,6 +308,8 @@ def test_batch_plan_classes_follow_the_table(gms_lib):
     assert plan([100, 512, 513]) == 1 + 2 + 1
     assert plan([100, 7, 0], B=5) == 1
     assert plan([100, 512], variant=2) == 2 + 1  # a forced tile shape keeps them tiled
+    # two scan groups (keys past 2^32) beside one-warp segments: 2 classes x 2 + 2 scans + 1
+    assert plan([(1 << 31) + 5, 100, (1 << 31) + 77, 50]) == 2 * 1 + 2 + 1
     arr = (batched.GmsSegment * 1)()
     arr[0] = batched.GmsSegment(fake, fake, fake, fake, 10, gms.delta_bucket().desc(256))
     h = ctypes.c_void_p()

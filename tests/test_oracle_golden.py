@@ -235,3 +235,38 @@ def test_oracle_more_than_256_buckets(oracle_mod):
             if o.ref_available():
                 rk, rv = o.ref_multisplit(keys, d, vals)
                 assert np.array_equal(rk, ko) and np.array_equal(rv, vo)
+
+
+def test_oracle_random_cases_against_numpy(oracle_mod):
+    """Seeded random cases (kind, B from 2 to 65536, n, skew): the oracle's
+    multisplit equals numpy's stable argsort of the ids numpy computes itself."""
+    o = oracle_mod
+    rng = np.random.default_rng(2024)
+    for trial in range(40):
+        B = int(rng.choice([2, 3, 7, 16, 100, 255, 256, 257, 1000, 4096, 65536]))
+        kind = int(rng.choice([o.DELTA, o.DIV, o.RANGE, o.MASK] + ([o.BITS] if B & (B - 1) == 0 else [])))
+        n = int(rng.integers(0, 5000))
+        keys = rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+        if trial % 3 == 0:
+            keys = keys & np.uint32(0xFFF0000F)  # many repeated high parts
+        k64 = keys.astype(np.uint64)
+        if kind == o.DELTA:
+            d, ids = o.Desc(o.DELTA, B), (k64 * B) >> 32
+        elif kind == o.DIV:
+            p = int(rng.integers(1, 2**20))
+            d, ids = o.Desc(o.DIV, B, param=p), (k64 // p) % B
+        elif kind == o.BITS:
+            sh = int(rng.integers(0, 32))
+            d, ids = o.Desc(o.BITS, B, shift=sh), (k64 >> sh) % B
+        elif kind == o.MASK:
+            m = int(rng.integers(1, 2**32))
+            d, ids = o.Desc(o.MASK, B, param=m), (k64 & m != 0).astype(np.uint64)
+        else:
+            spl = np.sort(rng.integers(0, 2**32, B, dtype=np.uint64)).astype(np.uint32)
+            ub = np.searchsorted(spl, keys, side="right").astype(np.int64) - 1
+            d, ids = o.Desc(o.RANGE, B, splitters=spl), np.where(ub < 0, B - 1, ub).astype(np.uint64)
+        vals = np.arange(n, dtype=np.uint32)
+        ko, vo, offs = o.multisplit(keys, d, vals)
+        order = np.argsort(ids, kind="stable")
+        assert np.array_equal(ko, keys[order]) and np.array_equal(vo, order.astype(np.uint32)), (trial, kind, B)
+        assert np.array_equal(offs, np.searchsorted(np.sort(ids), np.arange(B)).astype(np.uint32)), (trial, kind, B)
