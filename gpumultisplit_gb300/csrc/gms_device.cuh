@@ -24,15 +24,24 @@ enum DeviceError : uint32_t {
 
 // First 256 bytes of every scratch buffer.
 struct ScratchHeader {
-  uint32_t error;       // first DeviceError recorded in the current call
-  uint32_t error_info;  // block that recorded it
-  uint32_t ticket;      // scan chunk ticket counter
-  uint32_t reserved[61];
+  uint32_t error;          // first DeviceError recorded in the current call
+  uint32_t error_info;     // block that recorded it
+  uint32_t ticket;         // scan chunk ticket counter
+  uint32_t wait_limit_us;  // bound of every wait of the current call in microseconds (0: kWaitLimitNs)
+  uint32_t reserved[60];
 };
 static_assert(sizeof(ScratchHeader) == 256, "header is 256 bytes");
 
-// Wall-clock bound for every spin in the library (nanoseconds).
+// Default wall-clock bound for every spin in the library (nanoseconds).  A
+// call's prescan resets the header's wait_limit_us to 0, which selects it; a
+// shorter bound written between the stages of one call applies to that call's
+// scan and postscan.
 constexpr uint64_t kWaitLimitNs = 1000000000ull;  // 1 s
+
+__device__ __forceinline__ uint64_t wait_limit_ns(const ScratchHeader* h) {
+  const uint32_t us = *reinterpret_cast<const volatile uint32_t*>(&h->wait_limit_us);
+  return us != 0u ? uint64_t(us) * 1000ull : kWaitLimitNs;
+}
 
 __device__ __forceinline__ uint64_t global_timer_ns() {
   uint64_t t;
@@ -88,13 +97,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 
-// Wait for phase `parity` of an mbarrier, giving up after kWaitLimitNs.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// Wait for phase `parity` of an mbarrier, giving up after the call's wait
+// limit (the header's, read only when the first try fails).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, const ScratchHeader* h) {
   if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t limit = wait_limit_ns(h);
   const uint64_t t0 = global_timer_ns();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (global_timer_ns() - t0 > kWaitLimitNs) return false;
+    if (global_timer_ns() - t0 > limit) return false;
   }
 }
 

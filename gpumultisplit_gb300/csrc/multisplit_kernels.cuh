@@ -268,6 +268,7 @@ __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __r
     hdr->error = 0u;
     hdr->error_info = 0u;
     hdr->ticket = 0u;
+    hdr->wait_limit_us = 0u;
   }
 
   P::prepare(s_split, bp);
@@ -336,6 +337,7 @@ __global__ void __launch_bounds__(C::THREADS) prescan64_kernel(const uint64_t* _
     hdr->error = 0u;
     hdr->error_info = 0u;
     hdr->ticket = 0u;
+    hdr->wait_limit_us = 0u;
   }
 
   P::prepare(s_split, bp);
@@ -759,11 +761,11 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params, t
   }
   __syncthreads();
   if (bulk != 0) {
-    const bool ok = error_recorded(hdr) ? mbar_try_wait(s_bar, 0) : mbar_wait_bounded(s_bar, 0);
+    const bool ok = error_recorded(hdr) ? mbar_try_wait(s_bar, 0) : mbar_wait_bounded(s_bar, 0, hdr);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) {
         record_error(hdr, DEV_ERR_BULK_COPY_TIMEOUT);
-        mbar_wait_bounded(s_bar, 0);  // let a late copy land before the block moves on
+        mbar_wait_bounded(s_bar, 0, hdr);  // let a late copy land before the block moves on
       }
       return false;
     }

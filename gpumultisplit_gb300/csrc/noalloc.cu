@@ -11,10 +11,16 @@
 //
 // Limits and rules:
 //   * The array holds GMS_NOALLOC_SCRATCH_BYTES (4 MiB) on every GPU that loads
-//     the library, for the life of the process.  Calls whose scratch need
-//     (gms_multisplit_scratch_bytes(n, B, 1)) exceeds it are rejected with
-//     GMS_ERROR_SCRATCH_TOO_SMALL; at 256 buckets that is about 16 million pairs,
-//     at 2 buckets far more.
+//     the library, for the life of the process.  A call is accepted when the
+//     multisplit's minimum scratch (header, count matrix and scan status, without
+//     the optional byte per key) fits: up to 16,764,928 pairs at 256 buckets
+//     (4093 tiles of 4096), proportionally more at fewer buckets.  Larger calls
+//     are rejected with GMS_ERROR_SCRATCH_TOO_SMALL.  Costly identifiers (range,
+//     div, even-float) keep their byte per key in the array only when it also
+//     fits, and otherwise evaluate the identifier in both stages; the output is
+//     the same either way.  More than 256 buckets take two digit passes whose
+//     ping-pong keys and values also live in the array (about 460 thousand pairs
+//     at 1000 buckets).
 //   * The first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) with that device current; make that first call
 //     before any stream capture.
@@ -67,10 +73,15 @@ extern "C" gms_status gms_multisplit_key_value_noalloc(const uint32_t* d_key_in,
                                                        uint32_t* d_key_out, uint32_t* d_value_out, uint32_t n,
                                                        const gms_bucket_desc* desc, gms_stream_t stream) {
   if (desc == nullptr) return GMS_ERROR_INVALID_VALUE;
-  size_t need = 0;
-  gms_status st = gms_multisplit_scratch_bytes(n, desc->num_buckets, 1, &need);
-  if (st != GMS_SUCCESS) return st;
-  if (need > kNoAllocBytes) return GMS_ERROR_SCRATCH_TOO_SMALL;
+  // Up to 256 buckets the minimum scratch (without the byte per key) is what
+  // must fit; a call beyond it is rejected before the device is touched.  The
+  // wrapped entry point checks again (and, above 256 buckets, alone), and keeps
+  // bucket bytes only when they fit as well.
+  if (n != 0 && desc->num_buckets >= 2 && desc->num_buckets <= 256) {
+    int logb = 0;
+    while ((1u << logb) < desc->num_buckets) ++logb;
+    if (gms::make_geometry(n, logb, true).bytes > kNoAllocBytes) return GMS_ERROR_SCRATCH_TOO_SMALL;
+  }
   if (n == 0) return gms_multisplit_key_value(d_key_in, d_value_in, d_key_out, d_value_out, 0, desc, nullptr, 0,
                                               nullptr, stream);
   void* scratch = nullptr;

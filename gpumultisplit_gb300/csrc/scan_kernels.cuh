@@ -38,6 +38,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(uint32_t* __restrict
   if (tid == 0) s_chunk = atomicAdd(&hdr->ticket, 1u);
   __syncthreads();
   const uint32_t chunk = s_chunk;
+  // Tickets run from 0 when the prescan reset the counter; a block that draws
+  // one past the last chunk (a counter not reset) has nothing to scan.
+  if (chunk >= gridDim.x) return;
   const uint32_t first = chunk * SCAN_CHUNK + tid * SCAN_IPT;
 
   // Load 16 consecutive counts per thread (16-byte vectors when `data` is
@@ -89,7 +92,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(uint32_t* __restrict
       int64_t pred = int64_t(chunk) - 1;
       const uint64_t t0 = global_timer_ns();
       // After an error elsewhere in the call, give up on the first empty window.
-      const uint64_t limit = error_recorded(hdr) ? 0ull : kWaitLimitNs;
+      const uint64_t limit = error_recorded(hdr) ? 0ull : wait_limit_ns(hdr);
       bool timed_out = false;
       while (true) {
         const int64_t idx = pred - int64_t(lane);

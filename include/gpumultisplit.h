@@ -151,9 +151,13 @@ gms_status gms_multisplit_geometry(uint32_t n, uint32_t num_buckets, int key_val
  * (allocator internals, plugin hosts that hand over only input and output
  * buffers, paths that must not allocate after start-up).  Its scratch is a fixed
  * GMS_NOALLOC_SCRATCH_BYTES array in device memory owned by the library (held on
- * every GPU that loads the library until the process exits).  Calls that need
- * more scratch than that (gms_multisplit_scratch_bytes(n, B, 1) > the limit:
- * about 16 M pairs at 256 buckets) return GMS_ERROR_SCRATCH_TOO_SMALL.  The
+ * every GPU that loads the library until the process exits).  A call is accepted
+ * when the multisplit's minimum scratch (count matrix and scan state, without
+ * the optional byte per key) fits: up to 16,764,928 pairs at 256 buckets, more
+ * at fewer buckets, about 460 thousand at 1000 buckets (whose two digit passes
+ * also keep ping-pong keys and values there).  Larger calls return
+ * GMS_ERROR_SCRATCH_TOO_SMALL.  Range, div and even-float identifiers keep their
+ * byte per key in the array only when it fits too; the output is the same.  The
  * first call on a device looks up the array's address with that device
  * current; make it before any stream capture.  All calls on a device share the
  * array, so calls that overlap on the GPU race; each call resets what it reads.
