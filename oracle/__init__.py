@@ -27,7 +27,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libgms_ref.so"
-REF_SRC = Path(os.environ.get("GMS_REFERENCE_SRC", "/root/reference/src"))
+# The reference's source tree: GMS_REFERENCE_SRC, else the project checked out
+# beside this repository (../reference/src relative to the repository root).
+REF_SRC = Path(os.environ.get("GMS_REFERENCE_SRC", str(HERE.parent.parent / "reference" / "src")))
 
 DELTA, DIV, BITS, RANGE, MASK, EVEN_FLOAT = range(6)
 
