@@ -61,15 +61,17 @@ def parse():
     p.add_argument("--only-batched", action="store_true", help="print only the batched-form summary")
     p.add_argument("--only-tiny-segments", action="store_true",
                    help="print only the many-small-segments summary (one warp per segment against tiles)")
-    p.add_argument("--no-autotune", action="store_true",
-                   help="batched form: keep the built-in tile table instead of autotuning first")
+    p.add_argument("--autotune", action="store_true",
+                   help="batched form: autotune the tile table first instead of keeping the built-in one")
     p.add_argument("--no-serving", action="store_true", help="skip the serving-form measurement")
     p.add_argument("--only-serving", action="store_true", help="print only the serving-form summary")
-    p.add_argument("--serve-seconds", type=float, default=3.0)
+    p.add_argument("--serve-seconds", type=float, default=10.0)
     p.add_argument("--serve-rate", type=float, default=20000.0)
     p.add_argument("--sweep-part", default="all", choices=["all", "base", "wide", "big"],
                    help="with --sweep: all cases, or only the 32-bit cases (base), the 64-bit key / value cases "
                         "(wide) or the cases with more than 256 buckets (big)")
+    p.add_argument("--no-sweep", action="store_true",
+                   help="leave the 32-bit sweep (one entry per 2^28 case) out of the headline line")
     p.add_argument("--sweep", action="store_true",
                    help="time every 2^28 case of the key-value sweep, key-only, compaction, histogram and sort "
                         "(one JSON line per case) instead of the headline line")
@@ -174,6 +176,37 @@ class ClockSampler:
                 "power_w_max": max(pw) if pw else None, "samples": len(rows), "reasons": reasons}
 
 
+def bind_to_gpu_cpus(local: int) -> dict:
+    """Pins this process to the CPUs of the GPU's own NUMA node (the PCI
+    device's local_cpulist), so the pinned host buffers of the end-to-end steps
+    are allocated in the memory nearest the GPU rather than wherever the
+    process happened to start.  Returns what it did, for the JSON line."""
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(local), "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=30).stdout.strip()
+        dom, rest = bus.split(":", 1)
+        dev = f"/sys/bus/pci/devices/{dom[-4:].lower()}:{rest.lower()}"
+        with open(os.path.join(dev, "local_cpulist")) as f:
+            spec = f.read().strip()
+        cpus = set()
+        for part in spec.split(","):
+            a, _, b = part.partition("-")
+            cpus.update(range(int(a), int(b or a) + 1))
+        cpus &= os.sched_getaffinity(0)
+        if not cpus:
+            return {"cpus": None, "note": f"no usable CPU in {spec}"}
+        os.sched_setaffinity(0, cpus)
+        node = None
+        try:
+            with open(os.path.join(dev, "numa_node")) as f:
+                node = int(f.read().strip())
+        except (OSError, ValueError):
+            pass
+        return {"cpus": spec, "numa_node": node, "cpus_used": len(cpus)}
+    except (OSError, ValueError, subprocess.SubprocessError) as e:
+        return {"cpus": None, "note": f"not bound: {e}"}
+
+
 def hbm_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -253,6 +286,19 @@ def run_batched(dev, reps: int = 3, tune: bool = True):
     plan.run(use_graph=False)
     torch.cuda.synchronize()
     plain_ms, plain_wall = timed(plain_loop, reps)
+    # The same plain per-call loop captured into one CUDA graph: the plain
+    # path's device rate, with no host dispatch between the calls (every call
+    # is its three launches, one after the other on one stream).
+    plain_graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(plain_graph):
+        plain_loop()
+    plain_graph.replay()
+    torch.cuda.synchronize()
+    plain_graph_ms, _ = timed(plain_graph.replay, max(reps, 5))
+    kref.zero_()
+    vref.zero_()
+    plain_graph.replay()
+    torch.cuda.synchronize()
     graph_ms, _ = timed(lambda: plan.run(use_graph=True), max(reps, 5))
     nograph_ms, _ = timed(lambda: plan.run(use_graph=False), max(reps, 5))
     identical = bool(torch.equal(kout, kref) and torch.equal(vout, vref))
@@ -274,7 +320,10 @@ def run_batched(dev, reps: int = 3, tune: bool = True):
         "plain_per_call_ms": plain_ms,
         "plain_per_call_gkeys": total / (plain_ms * 1e-3) / 1e9,
         "plain_host_wall_ms": plain_wall,
+        "plain_graph_ms": plain_graph_ms,
+        "plain_graph_gkeys": total / (plain_graph_ms * 1e-3) / 1e9,
         "speedup_vs_plain": plain_ms / graph_ms,
+        "speedup_vs_plain_graph": plain_graph_ms / graph_ms,
         "batched_hbm_frac": 20.0 * total / (graph_ms * 1e-3) / 1e9 / peak,
         "launches_per_run": plan.launches,
         "plain_launches_per_run": 3 * len(sizes),
@@ -282,7 +331,77 @@ def run_batched(dev, reps: int = 3, tune: bool = True):
         "device_error": plan.device_error(),
     }
     plan.close()
+    del plain_graph
     del keys, vals, kout, vout, kref, vref, segs, plain
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_tuning_check(dev, reps: int = 10):
+    """Whether the tuning table matters: 4096 key-value segments with
+    log-uniform sizes in [1024, 65536] (seed 8), B in {2, 8, 32, 256}, delta or
+    range, run as one graph with (a) the built-in table (the plain path's
+    4096-key tile for every class), (b) tiles that just hold segments of up to
+    2048 keys (1024- and 2048-key tiles for the two smallest size classes),
+    (c) the table the autotuner measured on this device.  Outputs are compared
+    across the three."""
+    import torch
+
+    import gpumultisplit_gb300 as gms
+    from gpumultisplit_gb300 import datagen
+
+    sizes, buckets, kinds = datagen.batched_spec(seed=8, lo=1024, hi=65536)
+    starts = np.concatenate([[0], np.cumsum((sizes + 31) // 32 * 32)[:-1]]).astype(np.int64)
+    total_alloc = int(starts[-1] + (sizes[-1] + 31) // 32 * 32)
+    total = int(sizes.sum())
+    keys = datagen.uniform_u32(total_alloc, 12, device=dev)
+    vals = datagen.index_values(total_alloc, dev)
+    outs = [(torch.zeros_like(keys), torch.zeros_like(vals)) for _ in range(3)]
+    spl = {}
+
+    def segs(ko, vo):
+        out = []
+        for i, (n, B, kind) in enumerate(zip(sizes.tolist(), buckets.tolist(), kinds)):
+            o = int(starts[i])
+            if kind == "range" and i not in spl:
+                spl[i] = datagen.range_splitters(B, 2000 + i, dev)
+            ident = gms.delta_bucket() if kind == "delta" else gms.range_bucket(spl[i])
+            out.append(gms.Segment(keys[o:o + n], ko[o:o + n], n, B, ident, vals[o:o + n], vo[o:o + n]))
+        return out
+
+    def timed(plan):
+        plan.run(use_graph=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            plan.run(use_graph=True)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    saved = gms.tuning_table()
+    gms.reset_tuning()
+    builtin = gms.BatchedMultisplit(segs(*outs[0]))
+    gms.set_tuning({(B, True, c): v for B in (2, 8, 32, 256) for c, v in ((0, 2), (1, 1))})
+    small = gms.BatchedMultisplit(segs(*outs[1]))
+    gms.reset_tuning()
+    builtin_ms, small_ms = timed(builtin), timed(small)
+    t0 = time.perf_counter()
+    gms.autotune(buckets=(2, 8, 32, 256), key_value=(True,), keys_per_trial=1 << 25, reps=5)
+    tune_s = time.perf_counter() - t0
+    tuned = gms.BatchedMultisplit(segs(*outs[2]))
+    tuned_ms = timed(tuned)
+    same = all(bool(torch.equal(outs[0][0], o[0]) and torch.equal(outs[0][1], o[1])) for o in outs[1:])
+    for p in (builtin, small, tuned):
+        p.close()
+    gms.set_tuning(saved)
+    res = {"workload": f"{len(sizes)} key-value segments, sizes log-uniform in [1024, 65536] (seed 8), "
+                       f"B in {{2,8,32,256}}, delta or range; {total} pairs",
+           "builtin_table_ms": builtin_ms, "small_tiles_table_ms": small_ms, "tuned_table_ms": tuned_ms,
+           "autotune_s": tune_s, "builtin_vs_small_tiles": small_ms / builtin_ms,
+           "builtin_vs_tuned": tuned_ms / builtin_ms, "identical": same}
+    del keys, vals, outs
     torch.cuda.empty_cache()
     return res
 
@@ -303,8 +422,8 @@ def serving_trace(seconds: float, rate: float, seed: int = 5):
     return t, sizes, ops, kv, buckets
 
 
-def run_sweep(a, dev):
-    """One JSON line per case, inputs resident in HBM, CUDA events around
+def run_sweep(a, dev, out=None):
+    """One JSON line per case (appended to `out` instead when given), inputs resident in HBM, CUDA events around
     `steps` calls after `warmup` calls, each case's output checked by a
     size-independent property (bucket order + permutation for multisplits,
     sortedness for sorts, total count for histograms).  Beside each GPU figure,
@@ -365,7 +484,10 @@ def run_sweep(a, dev):
         if cpu is not None:
             line["cpu"] = cpu
             line["gpu_vs_cpu"] = line["gkeys"] / cpu["gkeys"]
-        print(json.dumps(line), flush=True)
+        if out is None:
+            print(json.dumps(line), flush=True)
+        else:
+            out.append(line)
 
     def bucket_ids(x, B, ident_name, spl):
         u = x.to(torch.int64) & 0xFFFFFFFF
@@ -441,8 +563,9 @@ def run_sweep(a, dev):
         ms = timed(lambda: gms.histogram_even(kin, n, hist, 256, 0, 0xFFFFFFFF, 256.0 / 2**32))
         emit("histogram 256 bins even-float uniform", ms, 4, "pass",
              cpu_rate(lambda: oracle.histogram(hk, oracle.Desc(oracle.EVEN_FLOAT, 256, inverse_delta=256.0 / 2**32)), 1))
-        # sorts
-        for bits in (7, 4, 5, 6, 8):
+        # sorts (the 7-bit ones by both digit methods)
+        for bits, method in ((7, "auto"), (7, "onesweep"), (4, "auto"), (5, "auto"), (6, "auto"), (8, "auto")):
+            gms.set_sort_method(method)
             for dist in (("uniform", "and4") if bits == 7 else ("uniform",)):
                 for kv in ((False, True) if bits == 7 else (True,)):
                     ctx = gms.ms_sort_context()
@@ -460,9 +583,11 @@ def run_sweep(a, dev):
                         ok &= bool(torch.equal(kin[vout.long()], kout))
                     passes = {4: 8, 5: 7, 6: 6, 7: 5, 8: 4}[bits]
                     hk, hv = sample(kin), (sample(vals) if kv else None)
-                    emit(f"sort {bits}-bit {'kv' if kv else 'k'} {dist}", ms, passes * (20 if kv else 12),
+                    label = " (one-sweep passes)" if method == "onesweep" else ""
+                    emit(f"sort {bits}-bit {'kv' if kv else 'k'} {dist}{label}", ms, passes * (20 if kv else 12),
                          "pass" if ok else "FAIL", cpu_rate(lambda: oracle.sort(hk, hv, bits), 1))
                     gms.multisplit_sort_release_memory(ctx)
+            gms.set_sort_method("auto")
     del inputs, kout, vout
     torch.cuda.empty_cache()
     if a.sweep_part in ("all", "wide"):
@@ -931,6 +1056,17 @@ def run_reference(a):
         times.append(time.perf_counter() - t0)
     tot = sum(times)
     value = a.steps * n / tot / 1e9
+    # The reference's CPU multisplit is single-threaded: the same algorithm on
+    # one core (oracle_multisplit, a restatement of cpu_multisplit_pairs_general),
+    # on the first 2^24 keys, best of 3.
+    m = min(n, 1 << 24)
+    k1, v1 = keys[:m], None if vals is None else vals[:m]
+    best = None
+    for _ in range(3):
+        t0 = time.perf_counter()
+        oracle.multisplit(k1, d, v1)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1e3 * tot / a.steps, "higher_is_better": True, "scaling": "weak",
@@ -940,6 +1076,11 @@ def run_reference(a):
                                    "(oracle/oracle.c oracle_multisplit_mt: the reference's "
                                    "cpu_multisplit_pairs_general algorithm, chunked across threads)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_baseline_1core": {"value": m / best / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"first 2^{m.bit_length() - 1} keys of the workload, best of 3, one thread "
+                                         "(oracle/oracle.c oracle_multisplit: the reference's single-threaded "
+                                         "cpu_multisplit_pairs_general; the reference's own build of that function "
+                                         "ran within 3 % of it on x86, where its sources are available)"},
     }
     print(json.dumps(line), flush=True)
 
@@ -986,9 +1127,10 @@ def host_link_gbs(h_src, d_buf, h_dst, dev, reps=3):
 
 
 def run_ours(a):
+    rank, world, local = dist_env()
+    affinity = bind_to_gpu_cpus(local)
     import torch
 
-    rank, world, local = dist_env()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     if a.only_batched or a.only_serving or a.only_tiny_segments:
@@ -998,7 +1140,7 @@ def run_ours(a):
         if a.only_tiny_segments:
             out = run_tiny_segments(dev)
         else:
-            out = (run_batched(dev, tune=not a.no_autotune) if a.only_batched
+            out = (run_batched(dev, tune=a.autotune) if a.only_batched
                    else run_serving(dev, a.serve_seconds, a.serve_rate))
         print(json.dumps(out), flush=True)
         return
@@ -1172,6 +1314,7 @@ def run_ours(a):
                "pipeline": "one-call API from pinned host buffers; steps alternate over 2 streams, keys and "
                            "values copied on their own streams, so a step's copies overlap its neighbours' work",
                "host_link": link,
+               "cpu_affinity": affinity,
                "link_frac": (nb / (e_ms * 1e-3) / 1e9) / link["concurrent_gbs_each"]}
         # every lane's last output is the same multisplit as the device-resident step
         ref_k = kout.cpu()
@@ -1203,9 +1346,19 @@ def run_ours(a):
     if not a.no_batched:
         del keys, vals, kout, vout
         torch.cuda.empty_cache()
-        line["batched"] = run_batched(dev, tune=not a.no_autotune)
+        line["batched"] = run_batched(dev, tune=a.autotune)
+        line["batched"]["tuning_check"] = run_tuning_check(dev)
     if not a.no_serving:
         line["serving"] = run_serving(dev, a.serve_seconds, a.serve_rate)
+    if not a.no_sweep:
+        # every 2^28 case of the 32-bit sweep (key-value B x identifier x
+        # distribution, key-only, compaction, histograms, sorts): one entry each
+        sw = argparse.Namespace(**vars(a))
+        sw.sweep_part = "base"
+        sw.steps, sw.warmup = 6, 3
+        cases = []
+        run_sweep(sw, dev, cases)
+        line["sweep"] = cases
     if rank == 0 and not a.no_cpu_baseline:
         keys, vals, _ = make_inputs(a, dev)
         line["cpu_baseline"] = cpu_baseline(a, keys, vals, a.cpu_seconds)

@@ -3,9 +3,12 @@
 // The batched form runs each segment with one of the tile variants of
 // kTileVariants (warps per block x keys per thread).  The table maps
 // (log2 B, key/value, segment size class) to a variant.  Its built-in entries
-// use the tile that just holds the segment for segments of up to 2048 keys and
-// the plain path's 4096-key tile otherwise; gms_autotune replaces them with
-// the variant that measured fastest on this device.
+// use the plain path's 4096-key tile for every class: on GB300, 4096 segments
+// of 1 Ki to 64 Ki pairs ran faster with it (0.374 ms) than with tiles that
+// just hold segments of up to 2048 keys (0.402 ms) or with the autotuned table
+// (0.410 ms).  gms_autotune, which is opt-in, replaces an entry with the
+// variant that measured fastest on this device on segments of that class
+// alone.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -21,9 +24,8 @@ namespace {
 
 constexpr int kMaxLogB = 8;
 
-// Built-in choice for a size class: the tile that just holds the segment up
-// to 2048 keys, the plain path's 4096-key tile above.
-int builtin_variant(int size_class_index) { return size_class_index == 0 ? 2 : (size_class_index == 1 ? 1 : 0); }
+// Built-in choice for every size class: the plain path's 4096-key tile.
+int builtin_variant(int) { return 0; }
 
 // Relative gain another variant needs over the built-in one to replace it.
 constexpr float kTuneMargin = 0.03f;

@@ -243,6 +243,19 @@ def test_partial_key_sort_scratch_and_checks(gms_lib):
             _lib.GMS_ERROR_INVALID_VALUE
 
 
+def test_sort_method_setting(gms_lib):
+    """gms_sort_set_method / get (host only): the three methods, and invalid values refused."""
+    v = ctypes.c_int()
+    assert gms_lib.gms_sort_get_method(ctypes.byref(v)) == 0 and v.value == _lib.GMS_SORT_AUTO
+    for m in ("multisplit", "onesweep", "auto"):
+        gms.set_sort_method(m)
+        assert gms.sort_method() == m
+    assert gms_lib.gms_sort_set_method(3) == _lib.GMS_ERROR_INVALID_VALUE
+    assert gms_lib.gms_sort_set_method(-1) == _lib.GMS_ERROR_INVALID_VALUE
+    assert gms_lib.gms_sort_get_method(None) == _lib.GMS_ERROR_INVALID_VALUE
+    assert gms.sort_method() == "auto"
+
+
 def test_tuning_table_host_logic(gms_lib):
     """Tile variants, the built-in table, set/get/reset and their checks (host only)."""
     from gpumultisplit_gb300 import batched
@@ -252,9 +265,9 @@ def test_tuning_table_host_logic(gms_lib):
     assert all(t == w * 32 * i for w, i, t in shapes)
     gms.reset_tuning()
     base = gms.tuning_table()
-    # built-in: the tile that holds the segment up to 2048 keys, the 4096-key tile above
+    # built-in: the plain path's 4096-key tile for every class
     for (b, kv, c), v in base.items():
-        assert gms.tile_variant_shape(v)[2] == {0: 1024, 1: 2048}.get(c, 4096)
+        assert gms.tile_variant_shape(v)[2] == 4096
     assert [batched.size_class(n) for n in (0, 1, 1024, 1025, 2048, 2049, 65536, 65537, 1 << 30)] == \
         [0, 0, 0, 1, 1, 2, 6, 7, 7]
     gms.set_tuning({(128, True, 3): 3})
@@ -297,11 +310,11 @@ def test_batch_plan_classes_follow_the_table(gms_lib):
         gms_lib.gms_batch_destroy(h)
         return n.value
 
-    assert plan([1000, 1000, 5000]) == 2 * 2 + 1        # 1024-key tiles and 4096-key tiles
-    assert plan([1000, 1500, 5000]) == 2 * 3 + 1
+    assert plan([1000, 1000, 5000]) == 2 + 1            # the built-in table: 4096-key tiles for every class
     assert plan([1000, 1500, 5000], variant=0) == 2 + 1
-    gms.set_tuning({(256, True, c): 0 for c in range(8)})
-    assert plan([1000, 1500, 5000]) == 2 + 1
+    gms.set_tuning({(256, True, 0): 2, (256, True, 1): 1})  # 1024-key tiles, 2048-key tiles, 4096 above
+    assert plan([1000, 1000, 5000]) == 2 * 2 + 1
+    assert plan([1000, 1500, 5000]) == 2 * 3 + 1
     gms.reset_tuning()
     # segments of at most 512 keys: one warp each, one launch per class, no scan
     assert plan([100, 512]) == 1
