@@ -35,6 +35,8 @@ from .api import (  # noqa: F401
     multisplit_stages,
     range_bucket,
     read_device_error,
+    set_sort_method,
+    sort_method,
     test_bucket,
 )
 from ._lib import GmsError, load  # noqa: F401

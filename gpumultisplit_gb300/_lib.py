@@ -17,6 +17,8 @@ GMS_ERROR_UNSUPPORTED_BUCKETS = 2
 GMS_ERROR_SCRATCH_TOO_SMALL = 3
 GMS_ERROR_CUDA = 4
 GMS_ERROR_DEVICE_TIMEOUT = 5
+# gms_sort_set_method
+GMS_SORT_AUTO, GMS_SORT_MULTISPLIT, GMS_SORT_ONESWEEP = 0, 1, 2
 GMS_ERROR_NOT_SUPPORTED = 6
 
 GMS_BUCKET_DELTA = 0
@@ -89,6 +91,8 @@ _PROTOS = {
     "gms_multisplit_postscan": [_P, _P, _P, _P, _U32, _PDESC, _P, _SZ, _P],
     "gms_multisplit_key_value_noalloc": [_P, _P, _P, _P, _U32, _PDESC, _P],
     "gms_sort_scratch_bytes": [_U32, _I32, _I32, _PSZ],
+    "gms_sort_set_method": [_I32],
+    "gms_sort_get_method": [ctypes.POINTER(ctypes.c_int)],
     "gms_sort_key_only": [_P, _P, _U32, _I32, _P, _SZ, _P],
     "gms_sort_key_value": [_P, _P, _P, _P, _U32, _I32, _P, _SZ, _P],
     "gms_sort_bits_scratch_bytes": [_U32, _I32, _I32, _I32, _I32, _PSZ],

@@ -394,6 +394,24 @@ def multisplit_sort_wide(d_key_in, d_key_out, n_elements: int, context, d_value_
                                     context.temp_storage_bytes, _stream(stream)), "multisplit_sort_wide")
 
 
+SORT_METHODS = {"auto": 0, "multisplit": 1, "onesweep": 2}
+
+
+def set_sort_method(method: str) -> None:
+    """How the 32-bit radix sorts run their digits, process-wide: "multisplit"
+    (prescan, scan, postscan per digit, the reference's way), "onesweep" (one
+    histogram pass, then one look-back pass per digit) or "auto" (the
+    library's choice, at present the multisplit passes).  The output is the
+    same either way."""
+    check(_lib.load().gms_sort_set_method(SORT_METHODS[method]), "gms_sort_set_method")
+
+
+def sort_method() -> str:
+    v = ctypes.c_int()
+    check(_lib.load().gms_sort_get_method(ctypes.byref(v)), "gms_sort_get_method")
+    return {v_: k for k, v_ in SORT_METHODS.items()}[v.value]
+
+
 def read_device_error(context, stream=None) -> int:
     """Device error word of a context's scratch (0 = every bounded wait finished)."""
     code = ctypes.c_uint32()

@@ -199,16 +199,34 @@ SortLayout sort_layout(uint32_t n, bool kv, const SortSchedule& sch) {
     const size_t b = make_geometry(n, logb, kv).bytes;
     L.ms_bytes = b > L.ms_bytes ? b : L.ms_bytes;
   }
+  // room for the one-sweep passes too, so either method can run on it
+  if (sch.passes <= kOnesweepMaxPasses) {
+    uint32_t logb[kOnesweepMaxPasses];
+    for (int p = 0; p < sch.passes; ++p) valid_buckets(sch.buckets[p], reinterpret_cast<int*>(&logb[p]));
+    const size_t b = onesweep_scratch_bytes(n, sch.passes, logb);
+    L.ms_bytes = b > L.ms_bytes ? b : L.ms_bytes;
+  }
   L.off_keys = align_up(L.ms_bytes, 256);
   L.off_vals = align_up(L.off_keys + size_t(n) * 4, 256);
   L.bytes = kv ? align_up(L.off_vals + size_t(n) * 4, 256) : L.off_vals;
   return L;
 }
 
+// Which way the 32-bit sorts run their digits (gms_sort_set_method).
+std::atomic<int> g_sort_method{GMS_SORT_AUTO};
+
+bool use_onesweep(uint32_t n, int passes) {
+  const int m = g_sort_method.load(std::memory_order_relaxed);
+  if (passes > kOnesweepMaxPasses || m == GMS_SORT_MULTISPLIT) return false;
+  return m == GMS_SORT_ONESWEEP || (n >= kOnesweepMinKeys && kOnesweepMinKeys != 0xFFFFFFFFu);
+}
+
 // LSD radix sort by stable multisplits on successive digits.  The buffers
 // ping-pong between the output and the scratch copy so the last pass lands in
 // the output (an odd number of passes starts in the output, an even one in the
-// copy), and the input is never written.
+// copy), and the input is never written.  From kOnesweepMinKeys keys up (or
+// as gms_sort_set_method says) the digits run as one-sweep passes
+// (onesweep.cu), with the same ping-pong and the same output.
 gms_status sort_run(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, uint32_t* vout, uint32_t n,
                     bool kv, const SortSchedule& sch, void* scratch, size_t scratch_bytes, cudaStream_t stream) {
   if (n == 0) return GMS_SUCCESS;
@@ -225,6 +243,23 @@ gms_status sort_run(const uint32_t* kin, uint32_t* kout, const uint32_t* vin, ui
   auto* base = static_cast<unsigned char*>(scratch);
   uint32_t* tk = reinterpret_cast<uint32_t*>(base + L.off_keys);
   uint32_t* tv = kv ? reinterpret_cast<uint32_t*>(base + L.off_vals) : nullptr;
+  if (use_onesweep(n, sch.passes)) {
+    // the same buffer checks as the multisplit passes make, pass by pass
+    const uint32_t* ki = kin;
+    const uint32_t* vi = vin;
+    for (int p = 0; p < sch.passes; ++p) {
+      const bool to_out = ((sch.passes - 1 - p) % 2) == 0;
+      uint32_t* ko = to_out ? kout : tk;
+      uint32_t* vo = to_out ? vout : tv;
+      if (overlaps(ki, ko, n) || (kv && (overlaps(vi, vo, n) || overlaps(ko, vo, n)))) return GMS_ERROR_INVALID_VALUE;
+      ki = ko;
+      vi = vo;
+    }
+    uint32_t logb[kOnesweepMaxPasses];
+    for (int p = 0; p < sch.passes; ++p) valid_buckets(sch.buckets[p], reinterpret_cast<int*>(&logb[p]));
+    return cuda_status(run_onesweep_sort(kin, kout, kv ? vin : nullptr, kv ? vout : nullptr, n, kv, sch.passes,
+                                         sch.shift, logb, base, tk, tv, stream));
+  }
   const uint32_t* ki = kin;
   const uint32_t* vi = vin;
   for (int p = 0; p < sch.passes; ++p) {
@@ -741,6 +776,19 @@ gms_status gms_multisplit_postscan(const uint32_t* d_key_in, const uint32_t* d_v
                                    void* d_scratch, size_t scratch_bytes, gms_stream_t stream) {
   return multisplit_impl(d_key_in, d_value_in, d_key_out, d_value_out, n, desc, d_value_in != nullptr, d_scratch,
                          scratch_bytes, STAGE_POSTSCAN, stream);
+}
+
+gms_status gms_sort_set_method(int method) {
+  if (method != GMS_SORT_AUTO && method != GMS_SORT_MULTISPLIT && method != GMS_SORT_ONESWEEP)
+    return GMS_ERROR_INVALID_VALUE;
+  g_sort_method.store(method, std::memory_order_relaxed);
+  return GMS_SUCCESS;
+}
+
+gms_status gms_sort_get_method(int* method) {
+  if (method == nullptr) return GMS_ERROR_INVALID_VALUE;
+  *method = g_sort_method.load(std::memory_order_relaxed);
+  return GMS_SUCCESS;
 }
 
 gms_status gms_sort_scratch_bytes(uint32_t max_elements, int digit_bits, int key_value, size_t* bytes) {

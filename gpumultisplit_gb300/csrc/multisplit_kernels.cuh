@@ -458,15 +458,36 @@ __device__ __forceinline__ uint32_t peers_by_ballot(uint32_t b) {
   return peers;
 }
 
+// Where a tile's global bucket offsets come from.  Thread b < B holds the
+// source for bucket b: aggregate() is called once the tile's count of bucket b
+// is known (after phase 2), offset() returns the bucket's global offset for
+// this tile after the tile is sorted in shared memory (phase 3), just before
+// the global stores.  GivenOffset is an entry of the scanned count matrix,
+// loaded when the tile starts.
+struct GivenOffset {
+  uint32_t goff;
+  __device__ __forceinline__ void aggregate(uint32_t, uint32_t) {}
+  __device__ __forceinline__ uint32_t offset(uint32_t, uint32_t) { return goff; }
+};
+
+// The default source of a job's offsets: its entries of the scanned count
+// matrix (minus the job's bias in a shared scan).
+struct MatrixOffsets {
+  template <class Job>
+  __device__ __forceinline__ GivenOffset operator()(const Job& job, uint32_t tid, uint32_t num_buckets) const {
+    return GivenOffset{tid < num_buckets ? job.offsets[tid * job.num_tiles + job.tile] - job.bias : 0u};
+  }
+};
+
 // Phases 1-4 of the postscan for one staged tile.  FULL: the tile holds
 // exactly TILE keys, so no per-key validity test is needed.
 //
 // GIVEN: the tile's buckets were staged as bytes at the bucket-byte area (in
 // input order) by the caller, so the identifier is not evaluated; phase 3
 // overwrites that area with the buckets in sorted order.
-template <class C, class P, bool FULL, bool GIVEN = false>
+template <class C, class P, bool FULL, bool GIVEN = false, class Offsets = GivenOffset>
 __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout, typename C::VT* __restrict__ vout,
-                                              uint32_t n, uint32_t cnt, uint32_t goff, const typename P::Params& bp,
+                                              uint32_t n, uint32_t cnt, Offsets& offs, const typename P::Params& bp,
                                               ScratchHeader* hdr, unsigned char* smem) {
   using L = PostLayout<C, P, GIVEN>;
   using WhT = typename L::WhT;
@@ -565,10 +586,10 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
   }
   __syncthreads();
 
-  // ---- 2. tile scan: per-warp offsets, bucket starts, and a range check of
-  // every bucket's output run against n (a corrupt offset matrix can then never
-  // cause a store outside the output).  Thread b owns bucket b; the bucket
-  // starts come from a block-wide exclusive scan (warp scans + warp totals).
+  // ---- 2. tile scan: per-warp offsets and bucket starts.  Thread b owns
+  // bucket b; the bucket starts come from a block-wide exclusive scan (warp
+  // scans + warp totals).
+  uint32_t my_total = 0, my_start = 0;
   {
     uint32_t total = 0;
     if (tid < B) {
@@ -579,7 +600,7 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
         *c_ptr = WhT(total);
         total += c;
       }
-      if (uint64_t(goff) + total > n) atomicOr(s_flag, 1u);
+      offs.aggregate(tid, total);
     }
     uint32_t incl = total;
 #pragma unroll
@@ -596,7 +617,8 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
 #pragma unroll
         for (uint32_t w = 0; w < SCAN_WARPS; ++w) start += (w < warp) ? s_scan[w] : 0u;
       }
-      s_delta[tid] = goff - start;
+      my_total = total;
+      my_start = start;
 #pragma unroll
       for (int w = 0; w < C::WARPS; ++w) {
         WhT* c_ptr = &s_wh[(w * WB + tid) * WS + (WS - 1)];
@@ -605,10 +627,6 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
     }
   }
   __syncthreads();
-  if (*s_flag != 0u) {  // block-uniform
-    if (tid == 0) record_error(hdr, DEV_ERR_BAD_OFFSET);
-    return false;
-  }
 
   // ---- 3. bucket-sorted in-tile order (positions are a permutation of [0, cnt))
   {
@@ -627,7 +645,19 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
       }
     }
   }
+  // The buckets' global offsets, the per-bucket shift delta = global offset -
+  // tile start, and a range check of every bucket's output run against n (a
+  // corrupt offset can then never cause a store outside the output).
+  if (tid < B) {
+    const uint32_t g = offs.offset(tid, my_total);
+    if (uint64_t(g) + my_total > n) atomicOr(s_flag, 1u);
+    s_delta[tid] = g - my_start;
+  }
   __syncthreads();
+  if (*s_flag != 0u) {  // block-uniform
+    if (tid == 0) record_error(hdr, DEV_ERR_BAD_OFFSET);
+    return false;
+  }
 
   // ---- 4. scatter in bucket-sorted order: each bucket's run is one coalesced store
 #pragma unroll
@@ -696,9 +726,13 @@ struct TileJob {
 // GIVEN: the prescan stored every key's bucket as a byte (job.bucket_bytes);
 // the tile's bytes are staged with its keys and the identifier is never
 // evaluated (nor prepared).
-template <class C, class P, bool PREPARE = true, bool GIVEN = false>
+//
+// make_offsets(job, tid, B) gives thread tid the source of bucket tid's global
+// offset (see GivenOffset); it is called while the tile's bulk copy is in flight.
+template <class C, class P, bool PREPARE = true, bool GIVEN = false, class MakeOffsets = MatrixOffsets>
 __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params, typename C::KT, typename C::VT>& job,
-                                             ScratchHeader* hdr, unsigned char* smem, bool* bar_live = nullptr) {
+                                             ScratchHeader* hdr, unsigned char* smem, bool* bar_live = nullptr,
+                                             MakeOffsets make_offsets = MakeOffsets()) {
   using L = PostLayout<C, P, GIVEN>;
   using KT = typename C::KT;
   using VT = typename C::VT;
@@ -752,7 +786,7 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params, t
     for (uint32_t i = bulk_b + tid; i < cnt; i += C::THREADS) s_rb[i] = job.bucket_bytes[base + i];
   }
   if (bar_live) *bar_live = bulk != 0;
-  const uint32_t goff = (tid < B) ? job.offsets[tid * job.num_tiles + job.tile] - job.bias : 0u;
+  auto offs = make_offsets(job, tid, B);
   if constexpr (PREPARE && !GIVEN) P::prepare(s_split, job.bp);
   if constexpr (LOGB > 5) {
     // the count table as 32-bit words (its byte size is a multiple of 4)
@@ -772,8 +806,8 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params, t
   }
 
   if (cnt == C::TILE)
-    return postscan_tile<C, P, true, GIVEN>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
-  return postscan_tile<C, P, false, GIVEN>(job.kout, job.vout, job.n, cnt, goff, job.bp, hdr, smem);
+    return postscan_tile<C, P, true, GIVEN>(job.kout, job.vout, job.n, cnt, offs, job.bp, hdr, smem);
+  return postscan_tile<C, P, false, GIVEN>(job.kout, job.vout, job.n, cnt, offs, job.bp, hdr, smem);
 }
 
 // Persistent postscan over tiles first, first + stride, ... below last, for

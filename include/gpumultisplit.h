@@ -196,6 +196,20 @@ gms_status gms_sort_key_value(const uint32_t* d_key_in, uint32_t* d_key_out, con
                               uint32_t* d_value_out, uint32_t n, int digit_bits, void* d_scratch,
                               size_t scratch_bytes, gms_stream_t stream);
 
+/* How the 32-bit radix sorts above and below run their digits (process-wide,
+ * default GMS_SORT_AUTO).  No counterpart in the reference, whose sorts run one
+ * multisplit per digit:
+ *   GMS_SORT_MULTISPLIT  prescan, scan and postscan per digit (the reference's way);
+ *   GMS_SORT_ONESWEEP    one histogram pass for every digit, then one pass per
+ *                        digit whose tiles find their offsets by decoupled
+ *                        look-back (no count matrix, no scan);
+ *   GMS_SORT_AUTO        the library's choice (at present the multisplit
+ *                        passes, which measured faster on GB300).
+ * Both give bit-identical output and fit the same scratch size. */
+enum { GMS_SORT_AUTO = 0, GMS_SORT_MULTISPLIT = 1, GMS_SORT_ONESWEEP = 2 };
+gms_status gms_sort_set_method(int method);
+gms_status gms_sort_get_method(int* method);
+
 /* Partial-key sorts: a stable sort by key bits [begin_bit, end_bit), as the
  * begin_bit / end_bit arguments of the CUB radix sorts the reference's drivers
  * compare against (src/main/main_bms.cu:199).  Digits of digit_bits (4..8)
