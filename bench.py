@@ -760,7 +760,7 @@ def run_tiny_segments(dev, count: int = 200000, seed: int = 9):
     return out
 
 def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: float = 64.0, verify: int = 24,
-                verify_all: bool = True):
+                verify_all: bool = True, plain_graph_sample: int = 2000, plain_loop: bool = True):
     """Serving form under Poisson arrivals against the plain per-request calls on
     the same trace: p50/p99 latency (arrival to result) and Gkeys/s.  With
     verify_all, every request of the trace is then served once more (untimed)
@@ -844,9 +844,13 @@ def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: floa
                                    desc_for(i)[1], None)
         if i % 64 == 0:
             reap()
-    lib.gms_server_drain(h)
+    # Reap (and release) until every request is done: a blocking drain would
+    # wait forever once unreleased results fill the arena (at saturation).
     while finished < m:
+        before = finished
         reap()
+        if finished == before:
+            time.sleep(5e-5)
     stats = server.stats()
     served_span = float(done_t.max() - t0)
     # verify the sampled requests against the plain calls alone
@@ -921,7 +925,7 @@ def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: floa
     vout = torch.empty(16 << 20, dtype=torch.int32, device=dev)
     hist = torch.empty(256, dtype=torch.int32, device=dev)
     tp0 = time.perf_counter() + 0.05
-    for i in range(m):
+    for i in (range(m) if plain_loop else ()):
         target = tp0 + t_arr[i]
         while time.perf_counter() < target:
             pass
@@ -933,6 +937,44 @@ def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: floa
         torch.cuda.synchronize()
         plain_lat[i] = time.perf_counter() - tp0 - t_arr[i]
     plain_span = time.perf_counter() - tp0
+
+    # ---- the plain per-request path's device rate: the first requests of the
+    # trace, each through its plain calls, captured into one CUDA graph and
+    # replayed back to back (no host dispatch, no arrival gaps).  A compaction
+    # is captured as its two-bucket multisplit: the plain call also reads the
+    # bucket-0 count back to the host, which a graph cannot.
+    plain_graph = None
+    if plain_graph_sample:
+        sample = range(min(plain_graph_sample, m))
+
+        def plain_calls():
+            for i in sample:
+                op, n = names[ops[i]], int(sizes[i])
+                kin = keys_pool[offs[i]:offs[i] + n]
+                vin = vals_pool[offs[i]:offs[i] + n] if reqs[i].d_value_in else None
+                if op == "compaction":
+                    op = "multisplit"
+                _plain_request(gms, op, kin, vin, n, desc_for(i)[1],
+                               gms.test_bucket(1) if names[ops[i]] == "compaction" else gms.delta_bucket(), ctxs,
+                               kout, vout, hist)
+
+        plain_calls()  # contexts exist before the capture
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            plain_calls()
+        graph.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            graph.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        g_ms = e0.elapsed_time(e1) / 3
+        g_keys = int(sizes[:len(sample)].sum())
+        plain_graph = {"requests": len(sample), "keys": g_keys, "ms": g_ms, "gkeys": g_keys / (g_ms * 1e-3) / 1e9}
+        del graph
     del keys_pool, vals_pool, kout, vout
     torch.cuda.empty_cache()
     return {
@@ -948,10 +990,11 @@ def run_serving(dev, seconds: float = 3.0, rate: float = 20000.0, arena_gb: floa
         # costs such as the staging buffers' first growth fall before it)
         "served_p50_ms_after_0p5s": float(np.percentile(lat[t_arr >= 0.5], 50) * 1e3) if (t_arr >= 0.5).any() else None,
         "served_p99_ms_after_0p5s": float(np.percentile(lat[t_arr >= 0.5], 99) * 1e3) if (t_arr >= 0.5).any() else None,
-        "plain_gkeys": total_keys / plain_span / 1e9,
-        "plain_p50_ms": float(np.percentile(plain_lat, 50) * 1e3),
-        "plain_p99_ms": float(np.percentile(plain_lat, 99) * 1e3),
-        "throughput_vs_plain": (total_keys / served_span) / (total_keys / plain_span),
+        "plain_gkeys": total_keys / plain_span / 1e9 if plain_loop else None,
+        "plain_p50_ms": float(np.percentile(plain_lat, 50) * 1e3) if plain_loop else None,
+        "plain_p99_ms": float(np.percentile(plain_lat, 99) * 1e3) if plain_loop else None,
+        "throughput_vs_plain": (total_keys / served_span) / (total_keys / plain_span) if plain_loop else None,
+        "plain_graph": plain_graph,
         "rounds": int(stats["rounds"]),
         "max_requests_in_round": int(stats["max_requests_in_round"]),
         "launches": int(stats["launches"]),
@@ -1350,6 +1393,14 @@ def run_ours(a):
         line["batched"]["tuning_check"] = run_tuning_check(dev)
     if not a.no_serving:
         line["serving"] = run_serving(dev, a.serve_seconds, a.serve_rate)
+        # the server's capacity: arrivals at 200,000/s for 0.5 s, far above what it carries
+        sat = run_serving(dev, 0.5, 200000.0, verify_all=False, plain_graph_sample=0, plain_loop=False)
+        pg = line["serving"]["plain_graph"]
+        line["serving"]["saturation"] = {
+            k: sat[k] for k in ("workload", "requests", "served_gkeys", "served_p50_ms", "served_p99_ms",
+                                "max_requests_in_round", "verified_identical")}
+        if pg:
+            line["serving"]["saturation"]["capacity_vs_plain_graph"] = sat["served_gkeys"] / pg["gkeys"]
     if not a.no_sweep:
         # every 2^28 case of the 32-bit sweep (key-value B x identifier x
         # distribution, key-only, compaction, histograms, sorts): one entry each

@@ -122,6 +122,9 @@ struct gms_server_s {
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   bool stop = false;
+  // Nothing on the GPU or admitted, and the oldest queued request does not fit
+  // the arena: only the caller's releases of finished results can free room.
+  bool blocked_on_release = false;
   std::thread worker;
   uint64_t next_id = 1;
   std::unordered_map<uint64_t, std::unique_ptr<gms::Request>> reqs;
@@ -418,6 +421,11 @@ void scheduler(gms_server_s* s) {
     progress |= admit(s);
     progress |= launch_round(s);
     s->stats.arena_peak_bytes = s->requests_arena.peak() + s->rounds_arena.peak();
+    const bool blocked = !s->queue.empty() && s->active.empty() && s->rounds.empty();
+    if (blocked != s->blocked_on_release) {
+      s->blocked_on_release = blocked;
+      if (blocked) s->cv_done.notify_all();  // drain and wait return instead of waiting forever
+    }
     if (s->stop && s->queue.empty() && s->active.empty() && s->rounds.empty()) break;
     if (progress) continue;
     if (!s->rounds.empty()) {
@@ -514,7 +522,8 @@ gms_status gms_server_wait(gms_server_t s, uint64_t id, gms_result* out) {
   auto it = s->reqs.find(id);
   if (it == s->reqs.end()) return GMS_ERROR_INVALID_VALUE;
   Request* q = it->second.get();
-  s->cv_done.wait(lock, [&] { return q->state == DONE; });
+  s->cv_done.wait(lock, [&] { return q->state == DONE || s->blocked_on_release; });
+  if (q->state != DONE) return GMS_ERROR_SCRATCH_TOO_SMALL;
   if (out) *out = q->res;
   return GMS_SUCCESS;
 }
@@ -543,8 +552,10 @@ gms_status gms_server_release(gms_server_t s, uint64_t id) {
 gms_status gms_server_drain(gms_server_t s) {
   if (s == nullptr) return GMS_ERROR_INVALID_VALUE;
   std::unique_lock<std::mutex> lock(s->mu);
-  s->cv_done.wait(lock, [&] { return s->queue.empty() && s->active.empty() && s->rounds.empty(); });
-  return GMS_SUCCESS;
+  s->cv_done.wait(lock, [&] {
+    return (s->queue.empty() && s->active.empty() && s->rounds.empty()) || s->blocked_on_release;
+  });
+  return s->queue.empty() && s->active.empty() && s->rounds.empty() ? GMS_SUCCESS : GMS_ERROR_SCRATCH_TOO_SMALL;
 }
 
 gms_status gms_server_get_stats(gms_server_t s, gms_server_stats* out) {

@@ -413,13 +413,18 @@ gms_status gms_server_create(void* d_arena, size_t arena_bytes, gms_server_t* se
 gms_status gms_server_submit(gms_server_t server, const gms_request* request, uint64_t* id);
 /* Current state of a request (result->done == 0 while pending). */
 gms_status gms_server_poll(gms_server_t server, uint64_t id, gms_result* result);
-/* Blocks until the request is done. */
+/* Blocks until the request is done.  Returns GMS_ERROR_SCRATCH_TOO_SMALL
+ * instead of waiting forever when the request is queued behind arena memory that
+ * only the caller can free: nothing is running and the finished results the
+ * caller has not released fill the arena.  Release results and wait again. */
 gms_status gms_server_wait(gms_server_t server, uint64_t id, gms_result* result);
 /* Ids of requests finished since the previous call (up to max). */
 gms_status gms_server_take_completed(gms_server_t server, uint64_t* ids, uint32_t max, uint32_t* count);
 /* Frees a finished request's arena memory and forgets it. */
 gms_status gms_server_release(gms_server_t server, uint64_t id);
-/* Blocks until every submitted request is done. */
+/* Blocks until every submitted request is done, or returns
+ * GMS_ERROR_SCRATCH_TOO_SMALL when the rest wait for arena memory held by
+ * finished results the caller has not released (see gms_server_wait). */
 gms_status gms_server_drain(gms_server_t server);
 gms_status gms_server_get_stats(gms_server_t server, gms_server_stats* stats);
 /* Seconds since the server was created (the clock of gms_result times). */

@@ -9,7 +9,7 @@ import pytest
 import torch
 
 import gpumultisplit_gb300 as gms
-from gpumultisplit_gb300 import datagen
+from gpumultisplit_gb300 import _lib, datagen
 
 pytestmark = pytest.mark.gpu
 
@@ -129,6 +129,41 @@ def test_admission_waits_for_budget(gms_lib):
     assert server.stats()["arena_peak_bytes"] <= arena
     with pytest.raises(gms.GmsError):  # can never fit
         server.submit("multisplit", keys[0], vals, 1 << 22, 256, gms.delta_bucket())
+    server.close()
+
+
+def test_drain_returns_when_only_releases_can_free_the_arena(gms_lib):
+    """Finished results the caller keeps fill the arena, so the queued rest can
+    never be admitted: drain and wait return GMS_ERROR_SCRATCH_TOO_SMALL instead
+    of blocking forever.  After the results are released, drain finishes the
+    rest, and every result is right."""
+    arena = 24 << 20
+    server = gms.Server(arena_bytes=arena)
+    n = 1 << 20  # 8 MiB of key-value output each: two fit the request part of the arena
+    keys = [datagen.uniform_u32(n, 80 + i, device="cuda") for i in range(6)]
+    vals = datagen.index_values(n, "cuda")
+    ids = [server.submit("multisplit", k, vals, n, 256, gms.delta_bucket()) for k in keys]
+    t0 = time.time()
+    with pytest.raises(gms.GmsError) as e:
+        server.drain()
+    assert e.value.status == _lib.GMS_ERROR_SCRATCH_TOO_SMALL
+    with pytest.raises(gms.GmsError) as e:
+        server.wait(ids[-1])
+    assert e.value.status == _lib.GMS_ERROR_SCRATCH_TOO_SMALL
+    assert time.time() - t0 < 30
+    checked = 0
+    while checked < len(ids):
+        done = server.take_completed()
+        for rid in done:
+            res = server.poll(rid)
+            i = ids.index(rid)
+            check(res, plain_result("multisplit", keys[i], vals, n, 256, gms.delta_bucket()), "multisplit")
+            server.release(rid)
+            checked += 1
+        if not done:
+            time.sleep(0.001)
+        assert time.time() - t0 < 60
+    server.drain()  # nothing left: returns at once
     server.close()
 
 
