@@ -460,11 +460,12 @@ __device__ __forceinline__ uint32_t peers_by_ballot(uint32_t b) {
 
 // Where a tile's global bucket offsets come from.  Thread b < B holds the
 // source for bucket b: aggregate() is called once the tile's count of bucket b
-// is known (after phase 2), offset() returns the bucket's global offset for
-// this tile after the tile is sorted in shared memory (phase 3), just before
-// the global stores.  GivenOffset is an entry of the scanned count matrix,
-// loaded when the tile starts.
+// is known (phase 2); offset() returns the bucket's global offset for this
+// tile, in phase 2 when KNOWN_EARLY, else after the tile is sorted in shared
+// memory (phase 3), just before the global stores.  GivenOffset is an entry of
+// the scanned count matrix, loaded when the tile starts.
 struct GivenOffset {
+  static constexpr bool KNOWN_EARLY = true;  // resolved in phase 2, before the reorder
   uint32_t goff;
   __device__ __forceinline__ void aggregate(uint32_t, uint32_t) {}
   __device__ __forceinline__ uint32_t offset(uint32_t, uint32_t) { return goff; }
@@ -601,6 +602,9 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
         total += c;
       }
       offs.aggregate(tid, total);
+      if constexpr (Offsets::KNOWN_EARLY) {
+        if (uint64_t(offs.offset(tid, total)) + total > n) atomicOr(s_flag, 1u);
+      }
     }
     uint32_t incl = total;
 #pragma unroll
@@ -617,8 +621,12 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
 #pragma unroll
         for (uint32_t w = 0; w < SCAN_WARPS; ++w) start += (w < warp) ? s_scan[w] : 0u;
       }
-      my_total = total;
-      my_start = start;
+      if constexpr (Offsets::KNOWN_EARLY) {
+        s_delta[tid] = offs.offset(tid, total) - start;
+      } else {
+        my_total = total;
+        my_start = start;
+      }
 #pragma unroll
       for (int w = 0; w < C::WARPS; ++w) {
         WhT* c_ptr = &s_wh[(w * WB + tid) * WS + (WS - 1)];
@@ -627,6 +635,12 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
     }
   }
   __syncthreads();
+  if constexpr (Offsets::KNOWN_EARLY) {
+    if (*s_flag != 0u) {  // block-uniform
+      if (tid == 0) record_error(hdr, DEV_ERR_BAD_OFFSET);
+      return false;
+    }
+  }
 
   // ---- 3. bucket-sorted in-tile order (positions are a permutation of [0, cnt))
   {
@@ -645,18 +659,23 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
       }
     }
   }
-  // The buckets' global offsets, the per-bucket shift delta = global offset -
-  // tile start, and a range check of every bucket's output run against n (a
-  // corrupt offset can then never cause a store outside the output).
-  if (tid < B) {
-    const uint32_t g = offs.offset(tid, my_total);
-    if (uint64_t(g) + my_total > n) atomicOr(s_flag, 1u);
-    s_delta[tid] = g - my_start;
+  // Offsets resolved only now: the buckets' global offsets, the per-bucket
+  // shift delta = global offset - tile start, and a range check of every
+  // bucket's output run against n (a corrupt offset can then never cause a
+  // store outside the output).
+  if constexpr (!Offsets::KNOWN_EARLY) {
+    if (tid < B) {
+      const uint32_t g = offs.offset(tid, my_total);
+      if (uint64_t(g) + my_total > n) atomicOr(s_flag, 1u);
+      s_delta[tid] = g - my_start;
+    }
   }
   __syncthreads();
-  if (*s_flag != 0u) {  // block-uniform
-    if (tid == 0) record_error(hdr, DEV_ERR_BAD_OFFSET);
-    return false;
+  if constexpr (!Offsets::KNOWN_EARLY) {
+    if (*s_flag != 0u) {  // block-uniform
+      if (tid == 0) record_error(hdr, DEV_ERR_BAD_OFFSET);
+      return false;
+    }
   }
 
   // ---- 4. scatter in bucket-sorted order: each bucket's run is one coalesced store

@@ -131,6 +131,7 @@ __global__ void __launch_bounds__(256) onesweep_bases_kernel(uint32_t* __restric
 // by the call's wait limit; on timeout the error is recorded and the tile
 // still publishes, so no later tile waits forever.
 struct LookbackOffset {
+  static constexpr bool KNOWN_EARLY = false;  // resolved after the shared-memory reorder
   uint64_t* status;  // this digit's words, [tile][B]
   uint32_t tile;
   uint32_t num_buckets;
