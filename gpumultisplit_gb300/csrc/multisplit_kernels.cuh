@@ -592,13 +592,21 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
   // scans + warp totals).
   uint32_t my_total = 0, my_start = 0;
   {
+    // Key-value tiles keep the per-warp prefixes in registers across the block
+    // scan and write each count-table entry once; key-only tiles, budgeted at
+    // 40 registers, write the prefixes and add the start in a second pass.
+    constexpr bool PREFIX_IN_REGS = C::KV;
+    uint32_t pre[PREFIX_IN_REGS ? C::WARPS : 1];
     uint32_t total = 0;
     if (tid < B) {
 #pragma unroll
       for (int w = 0; w < C::WARPS; ++w) {
         WhT* c_ptr = &s_wh[(w * WB + tid) * WS + (WS - 1)];
         const uint32_t c = *c_ptr;
-        *c_ptr = WhT(total);
+        if constexpr (PREFIX_IN_REGS)
+          pre[w] = total;
+        else
+          *c_ptr = WhT(total);
         total += c;
       }
       offs.aggregate(tid, total);
@@ -630,7 +638,10 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
 #pragma unroll
       for (int w = 0; w < C::WARPS; ++w) {
         WhT* c_ptr = &s_wh[(w * WB + tid) * WS + (WS - 1)];
-        *c_ptr = WhT(*c_ptr + start);
+        if constexpr (PREFIX_IN_REGS)
+          *c_ptr = WhT(pre[w] + start);
+        else
+          *c_ptr = WhT(*c_ptr + start);
       }
     }
   }
