@@ -306,6 +306,18 @@ def run_batched(dev, reps: int = 3, tune: bool = True):
     fixed_ms, _ = timed(lambda: plan_fixed.run(use_graph=True), max(reps, 5))
     identical = identical and bool(torch.equal(kout, kref) and torch.equal(vout, vref))
     plan_fixed.close()
+    # The same segments as one persistent launch over a device-side work list.
+    kout.zero_()
+    vout.zero_()
+    plan_queue = gms.BatchedMultisplit(segs, schedule="queue")
+    plan_queue.run(use_graph=True)
+    torch.cuda.synchronize()
+    queue_identical = bool(torch.equal(kout, kref) and torch.equal(vout, vref))
+    queue_ms, _ = timed(lambda: plan_queue.run(use_graph=True), max(reps, 5))
+    queue_identical = queue_identical and bool(torch.equal(kout, kref) and torch.equal(vout, vref))
+    queue_error = plan_queue.device_error()
+    queue_launches = plan_queue.launches
+    plan_queue.close()
     peak, _ = hbm_peak()
     res = {
         "workload": f"{len(sizes)} key-value segments, sizes log-uniform in [1024, 4194304] (seed 7), "
@@ -329,6 +341,17 @@ def run_batched(dev, reps: int = 3, tune: bool = True):
         "plain_launches_per_run": 3 * len(sizes),
         "identical_to_plain": identical,
         "device_error": plan.device_error(),
+        "queue": {
+            "schedule": "one persistent launch over a device-side work list (gms_batch_set_schedule QUEUE)",
+            "ms": queue_ms,
+            "gkeys": total / (queue_ms * 1e-3) / 1e9,
+            "hbm_frac": 20.0 * total / (queue_ms * 1e-3) / 1e9 / peak,
+            "vs_classes_graph": graph_ms / queue_ms,
+            "speedup_vs_plain_graph": plain_graph_ms / queue_ms,
+            "launches_per_run": queue_launches,
+            "identical_to_plain": queue_identical,
+            "device_error": queue_error,
+        },
     }
     plan.close()
     del plain_graph

@@ -19,6 +19,7 @@ GMS_ERROR_CUDA = 4
 GMS_ERROR_DEVICE_TIMEOUT = 5
 # gms_sort_set_method
 GMS_SORT_AUTO, GMS_SORT_MULTISPLIT, GMS_SORT_ONESWEEP = 0, 1, 2
+GMS_BATCH_SCHEDULE_CLASSES, GMS_BATCH_SCHEDULE_QUEUE = 0, 1
 GMS_ERROR_NOT_SUPPORTED = 6
 
 GMS_BUCKET_DELTA = 0
@@ -115,6 +116,8 @@ _PROTOS = {
     "gms_batch_launch_count": [_P, _PU32],
     "gms_batch_destroy": [_P],
     "gms_batch_create_with_variant": [_P, _U32, _I32, _P],
+    "gms_batch_set_schedule": [_P, _I32],
+    "gms_batch_get_schedule": [_P, ctypes.POINTER(ctypes.c_int)],
     "gms_tile_variant_shape": [_I32, _PU32, _PU32, _PU32],
     "gms_tuning_get": [_U32, _I32, _I32, ctypes.POINTER(ctypes.c_int)],
     "gms_tuning_set": [_U32, _I32, _I32, _I32],

@@ -109,9 +109,10 @@ def autotune(buckets=(2, 4, 8, 16, 32, 64, 128, 256), key_value=(False, True), k
 class BatchedMultisplit:
     """A plan over a list of Segment; run() executes every segment's multisplit.
     variant=None takes each segment's tile shape from the tuning table; an int
-    forces that tile variant for every segment."""
+    forces that tile variant for every segment (the "classes" schedule).
+    schedule: "classes" or "queue" (see the `schedule` property)."""
 
-    def __init__(self, segments: list[Segment], variant: int | None = None):
+    def __init__(self, segments: list[Segment], variant: int | None = None, schedule: str = "classes"):
         lib = _lib.load()
         self._segments = list(segments)
         arr = (GmsSegment * max(1, len(segments)))()
@@ -132,6 +133,24 @@ class BatchedMultisplit:
         check(lib.gms_batch_scratch_bytes(self._handle, ctypes.byref(nbytes)), "gms_batch_scratch_bytes")
         self.scratch_bytes = nbytes.value
         self.scratch = _alloc_scratch(nbytes.value)
+        if schedule != "classes":
+            self.schedule = schedule
+
+    SCHEDULES = {"classes": _lib.GMS_BATCH_SCHEDULE_CLASSES, "queue": _lib.GMS_BATCH_SCHEDULE_QUEUE}
+
+    @property
+    def schedule(self) -> str:
+        """"classes": one prescan and postscan launch per segment class (the
+        default); "queue": one persistent launch over a device-side work list."""
+        v = ctypes.c_int()
+        check(_lib.load().gms_batch_get_schedule(self._handle, ctypes.byref(v)), "gms_batch_get_schedule")
+        return {c: n for n, c in self.SCHEDULES.items()}[v.value]
+
+    @schedule.setter
+    def schedule(self, name: str) -> None:
+        if name not in self.SCHEDULES:
+            raise ValueError(f"schedule must be one of {sorted(self.SCHEDULES)}")
+        check(_lib.load().gms_batch_set_schedule(self._handle, self.SCHEDULES[name]), "gms_batch_set_schedule")
 
     @property
     def launches(self) -> int:

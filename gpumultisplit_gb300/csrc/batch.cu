@@ -55,6 +55,15 @@ struct gms_batch_s {
   // several streams so small classes overlap large ones (created on first use).
   std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> events;
+  // The one-launch schedule (batch_queue.cuh): segment records and work list
+  // (tables, uploaded with the class tables), then its run-time regions,
+  // which overlay the class schedule's (a run uses one schedule).
+  int schedule = GMS_BATCH_SCHEDULE_CLASSES;
+  bool queue_ok = false;  // the queue's count matrix fits 32-bit offsets
+  std::vector<gms::QSeg> qsegs;
+  std::vector<uint2> qitems;
+  size_t off_qsegs = 0, off_qitems = 0;
+  size_t off_qmatrix = 0, off_qstate = 0, off_qstatus = 0, off_qbytes = 0, q_state_bytes = 0;
 };
 
 namespace gms {
@@ -191,6 +200,154 @@ cudaError_t launch_all(gms_batch_s* b, unsigned char* scratch, cudaStream_t s, b
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+// Order of the queue's work list.  Counting (PRE) tiles run this many tiles
+// ahead of reordering (POST) tiles, so a segment's keys are read again about
+// 4 MiB of other keys after they were counted, usually still from L2.
+#ifndef GMS_QUEUE_LEAD_TILES
+#define GMS_QUEUE_LEAD_TILES 256
+#endif
+// A segment's first POST item comes at least this many resident blocks' worth
+// of items (two waves) after its last SCAN item, so its scan has finished by
+// the time its POST items are claimed and they rarely wait.
+constexpr uint32_t kQueueScanGapWaves = 2;
+
+// The queue's records and work list for the segments (the class plan's
+// descriptors give pointers, n and identifier parameters).  Segments are taken
+// class by class, largest first.  PRE items of a segment are followed by its SCAN items; the
+// list then takes the next POST tile (in segment order) whenever that
+// segment's SCAN items are far enough back and the PRE frontier leads the POST
+// frontier by GMS_QUEUE_LEAD_TILES tiles, else the next PRE or SCAN item.
+// Returns false when a count matrix would need offsets of 2^32 or more.
+bool build_queue(gms_batch_s* b, const gms_segment* segments, uint32_t count, uint64_t* matrix_words,
+                 uint64_t* chunks_total, uint64_t* byte_total) {
+  b->qsegs.assign(count, QSeg{});
+  b->qitems.clear();
+  uint64_t m_total = 0, c_total = 0, bytes = 0;
+  for (uint32_t i = 0; i < count; ++i) {
+    const gms_segment& sg = segments[i];
+    int logb = 0;
+    log2_buckets(sg.desc.num_buckets, &logb);
+    QSeg& q = b->qsegs[i];
+    q.d = b->segs[i];
+    q.d.num_tiles = uint32_t((uint64_t(sg.n) + QUEUE_TILE - 1) / QUEUE_TILE);
+    q.d.base = 0;
+    q.d.matrix_off = uint32_t(m_total);
+    const uint64_t m = uint64_t(q.d.num_tiles) << logb;
+    m_total = (m_total + m + 3) & ~uint64_t(3);  // every segment's counts start on 16 bytes
+    if (m_total > 0xFFFFFFFFull) return false;
+    q.d.bytes_off = 0;
+    if (sg.desc.kind != KIND_DELTA && sg.n > 0) {
+      q.d.bytes_off = bytes;
+      bytes += (uint64_t(sg.n) + 15) & ~uint64_t(15);
+    }
+    q.chunks = uint32_t((m + kScanChunk - 1) / kScanChunk);
+    q.status_off = uint32_t(c_total);
+    c_total += q.chunks;
+    q.meta = uint32_t(sg.desc.kind) | (uint32_t(logb) << 8) | (sg.d_value_in != nullptr ? 1u << 16 : 0u);
+  }
+  std::vector<uint32_t> order;
+  for (uint32_t i = 0; i < count; ++i)
+    if (segments[i].n > 0) order.push_back(i);
+  // Segments of one class (identifier kind, bucket count, key/value) run
+  // together, largest first, so the blocks running at once mostly execute
+  // the same code; the classes with the most keys come first.
+  std::map<uint32_t, uint64_t> class_keys;
+  for (uint32_t i : order) class_keys[b->qsegs[i].meta] += segments[i].n;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+    const uint32_t cx = b->qsegs[x].meta, cy = b->qsegs[y].meta;
+    if (cx != cy) return class_keys[cx] != class_keys[cy] ? class_keys[cx] > class_keys[cy] : cx < cy;
+    return segments[x].n > segments[y].n;
+  });
+  // PRE and SCAN items in order; the POST tiles are merged in below.
+  std::vector<uint2> first_stage;
+  for (uint32_t i : order) {
+    const QSeg& q = b->qsegs[i];
+    for (uint32_t g = 0; g * QUEUE_PRE_TILES < q.d.num_tiles; ++g)
+      first_stage.push_back(make_uint2(i, (QITEM_PRE << QITEM_SHIFT) | g));
+    for (uint32_t c = 0; c < q.chunks; ++c) first_stage.push_back(make_uint2(i, (QITEM_SCAN << QITEM_SHIFT) | c));
+  }
+  const uint64_t gap = uint64_t(kQueueScanGapWaves) * uint64_t(std::max(1, device_sm_count())) * QUEUE_MIN_BLOCKS;
+  // List position of a segment's last SCAN item, once every one of them is listed.
+  std::vector<uint64_t> last_scan(count, ~uint64_t(0));
+  uint64_t pre_tiles = 0, post_tiles = 0;
+  size_t fi = 0, post_seg = 0;
+  uint32_t post_tile = 0;
+  while (fi < first_stage.size() || post_seg < order.size()) {
+    bool post = false;
+    if (post_seg < order.size()) {
+      const uint32_t s = order[post_seg];
+      const bool scanned = last_scan[s] != ~uint64_t(0) && b->qitems.size() - last_scan[s] >= gap;
+      post = fi >= first_stage.size() || (scanned && pre_tiles >= post_tiles + GMS_QUEUE_LEAD_TILES);
+    }
+    if (post) {
+      const uint32_t s = order[post_seg];
+      b->qitems.push_back(make_uint2(s, (QITEM_POST << QITEM_SHIFT) | post_tile));
+      ++post_tiles;
+      if (++post_tile == b->qsegs[s].d.num_tiles) {
+        ++post_seg;
+        post_tile = 0;
+      }
+    } else {
+      const uint2 it = first_stage[fi++];
+      const QSeg& q = b->qsegs[it.x];
+      const uint32_t idx = it.y & ((1u << QITEM_SHIFT) - 1u);
+      if ((it.y >> QITEM_SHIFT) == QITEM_PRE)
+        pre_tiles += std::min<uint32_t>(QUEUE_PRE_TILES, q.d.num_tiles - idx * QUEUE_PRE_TILES);
+      else if (idx + 1 == q.chunks)
+        last_scan[it.x] = b->qitems.size();
+      b->qitems.push_back(it);
+    }
+  }
+  // Every item may wait only on items listed before it (the launch relies on
+  // that to make progress): each segment's PRE items before its SCAN items,
+  // all of them before its first POST item.  A list that breaks this is never
+  // launched.
+  std::vector<uint32_t> pre_seen(count, 0), scan_seen(count, 0);
+  for (const uint2& it : b->qitems) {
+    const QSeg& q = b->qsegs[it.x];
+    const uint32_t type = it.y >> QITEM_SHIFT;
+    if (type == QITEM_PRE) {
+      if (scan_seen[it.x] != 0) return false;
+      pre_seen[it.x] += std::min<uint32_t>(QUEUE_PRE_TILES, q.d.num_tiles - (it.y & ((1u << QITEM_SHIFT) - 1u)) * QUEUE_PRE_TILES);
+    } else if (type == QITEM_SCAN) {
+      if (pre_seen[it.x] != q.d.num_tiles) return false;
+      ++scan_seen[it.x];
+    } else if (scan_seen[it.x] != q.chunks) {
+      return false;
+    }
+  }
+  *matrix_words = m_total;
+  *chunks_total = c_total;
+  *byte_total = bytes;
+  return true;
+}
+
+// One run of the queue schedule: reset the header and the run state, then the
+// one launch.
+cudaError_t launch_queue(gms_batch_s* b, unsigned char* scratch, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(ScratchHeader), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(scratch + b->off_qstate, 0, b->q_state_bytes, s);
+  if (e != cudaSuccess) return e;
+  BatchQueueLaunch L;
+  L.qsegs = reinterpret_cast<const QSeg*>(scratch + b->off_qsegs);
+  L.items = reinterpret_cast<const uint2*>(scratch + b->off_qitems);
+  L.num_items = uint32_t(b->qitems.size());
+  L.num_segs = uint32_t(b->qsegs.size());
+  L.matrix = reinterpret_cast<uint32_t*>(scratch + b->off_qmatrix);
+  L.byte_area = scratch + b->off_qbytes;
+  L.state = reinterpret_cast<uint32_t*>(scratch + b->off_qstate);
+  L.status = reinterpret_cast<uint64_t*>(scratch + b->off_qstatus);
+  L.hdr = reinterpret_cast<ScratchHeader*>(scratch);
+  L.stream = s;
+  return run_batch_queue(L);
+}
+
+// The launch sequence of the batch's current schedule.
+cudaError_t launch_schedule(gms_batch_s* b, unsigned char* scratch, cudaStream_t s, bool fork) {
+  if (b->schedule == GMS_BATCH_SCHEDULE_QUEUE) return launch_queue(b, scratch, s);
+  return launch_all(b, scratch, s, fork);
 }
 
 }  // namespace
@@ -339,11 +496,33 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
     c.map_off = off;
     off = align_up(off + c.map_bytes(), 256);
   }
+  uint64_t q_matrix = 0, q_chunks = 0, q_bytes = 0;
+  b->queue_ok = build_queue(b, segments, count, &q_matrix, &q_chunks, &q_bytes);
+  if (b->queue_ok) {
+    b->off_qsegs = off;
+    off = align_up(off + b->qsegs.size() * sizeof(QSeg), 256);
+    b->off_qitems = off;
+    off = align_up(off + b->qitems.size() * sizeof(uint2), 256);
+  } else {
+    b->qsegs.clear();
+    b->qitems.clear();
+  }
+  const size_t run_start = off;  // run-time regions of either schedule start here
   b->off_matrix = off;
   off = align_up(off + size_t(matrix_total) * 4, 256);
   b->off_status = off;
   b->off_bytes = align_up(off + size_t(b->max_chunks) * 8, 256);
   b->bytes = align_up(b->off_bytes + size_t(byte_total), 256);
+  if (b->queue_ok) {
+    size_t q = run_start;
+    b->off_qmatrix = q;
+    q = align_up(q + size_t(q_matrix) * 4, 256);
+    b->off_qstate = q;  // ticket, PRE tiles done and SCAN chunks done per segment, then the look-back words
+    b->off_qstatus = align_up(q + (1 + 2 * size_t(count)) * 4, 16);
+    b->q_state_bytes = b->off_qstatus + size_t(q_chunks) * 8 - b->off_qstate;
+    b->off_qbytes = align_up(b->off_qstatus + size_t(q_chunks) * 8, 256);
+    b->bytes = std::max(b->bytes, align_up(b->off_qbytes + size_t(q_bytes), 256));
+  }
   *batch = b;
   return GMS_SUCCESS;
 }
@@ -372,10 +551,37 @@ gms_status gms_batch_scratch_bytes(gms_batch_t batch, size_t* bytes) {
 
 gms_status gms_batch_launch_count(gms_batch_t batch, uint32_t* launches) {
   if (batch == nullptr || launches == nullptr) return GMS_ERROR_INVALID_VALUE;
+  if (batch->schedule == GMS_BATCH_SCHEDULE_QUEUE) {
+    *launches = batch->qitems.empty() ? 0u : 1u;
+    return GMS_SUCCESS;
+  }
   uint32_t n = 0;
   for (const BatchClass& c : batch->classes) n += c.warp ? 1u : (c.tiles.empty() ? 0u : 2u);
   for (const ScanGroup& g : batch->groups) n += g.m > 0 ? 1u : 0u;
   *launches = n;
+  return GMS_SUCCESS;
+}
+
+gms_status gms_batch_set_schedule(gms_batch_t batch, int schedule) {
+  if (batch == nullptr || (schedule != GMS_BATCH_SCHEDULE_CLASSES && schedule != GMS_BATCH_SCHEDULE_QUEUE))
+    return GMS_ERROR_INVALID_VALUE;
+  if (schedule == GMS_BATCH_SCHEDULE_QUEUE && !batch->queue_ok) return GMS_ERROR_NOT_SUPPORTED;
+  std::lock_guard<std::mutex> lock(batch->mu);
+  if (batch->schedule != schedule) {
+    // The captured graph holds the other schedule's launches.
+    if (batch->exec) cudaGraphExecDestroy(batch->exec);
+    if (batch->graph) cudaGraphDestroy(batch->graph);
+    batch->exec = nullptr;
+    batch->graph = nullptr;
+    batch->graph_scratch = nullptr;
+    batch->schedule = schedule;
+  }
+  return GMS_SUCCESS;
+}
+
+gms_status gms_batch_get_schedule(gms_batch_t batch, int* schedule) {
+  if (batch == nullptr || schedule == nullptr) return GMS_ERROR_INVALID_VALUE;
+  *schedule = batch->schedule;
   return GMS_SUCCESS;
 }
 
@@ -396,13 +602,20 @@ gms_status gms_batch_run(gms_batch_t b, void* d_scratch, size_t scratch_bytes, i
       const BatchClass& c = b->classes[i];
       e = cudaMemcpyAsync(scratch + c.map_off, c.map_data(), c.map_bytes(), cudaMemcpyHostToDevice, stream);
     }
+    if (e == cudaSuccess && b->queue_ok) {
+      e = cudaMemcpyAsync(scratch + b->off_qsegs, b->qsegs.data(), b->qsegs.size() * sizeof(QSeg),
+                          cudaMemcpyHostToDevice, stream);
+      if (e == cudaSuccess && !b->qitems.empty())
+        e = cudaMemcpyAsync(scratch + b->off_qitems, b->qitems.data(), b->qitems.size() * sizeof(uint2),
+                            cudaMemcpyHostToDevice, stream);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return to_status(e);
     b->bound = d_scratch;
   }
   e = ensure_side_streams(b);
   if (e != cudaSuccess) return to_status(e);
-  if (!use_graph) return to_status(launch_all(b, scratch, stream, true));
+  if (!use_graph) return to_status(launch_schedule(b, scratch, stream, true));
 
   if (b->exec == nullptr || b->graph_scratch != d_scratch) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -415,7 +628,7 @@ gms_status gms_batch_run(gms_batch_t b, void* d_scratch, size_t scratch_bytes, i
     }
     e = cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return to_status(e);
-    const cudaError_t le = launch_all(b, scratch, b->capture_stream, true);
+    const cudaError_t le = launch_schedule(b, scratch, b->capture_stream, true);
     e = cudaStreamEndCapture(b->capture_stream, &b->graph);
     if (le != cudaSuccess) return to_status(le);
     if (e != cudaSuccess) return to_status(e);
@@ -444,9 +657,13 @@ gms_status batch_run_async(gms_batch_t b, void* d_scratch, size_t scratch_bytes,
   std::memcpy(staging, b->segs.data(), b->segs.size() * sizeof(SegDesc));
   for (const BatchClass& c : b->classes)
     std::memcpy(staging + (c.map_off - b->off_segs), c.map_data(), c.map_bytes());
+  if (b->queue_ok) {
+    std::memcpy(staging + (b->off_qsegs - b->off_segs), b->qsegs.data(), b->qsegs.size() * sizeof(QSeg));
+    std::memcpy(staging + (b->off_qitems - b->off_segs), b->qitems.data(), b->qitems.size() * sizeof(uint2));
+  }
   auto* scratch = static_cast<unsigned char*>(d_scratch);
   cudaError_t e = cudaMemcpyAsync(scratch + b->off_segs, staging, table, cudaMemcpyHostToDevice, stream);
-  if (e == cudaSuccess) e = launch_all(b, scratch, stream);
+  if (e == cudaSuccess) e = launch_schedule(b, scratch, stream, false);
   return to_status(e);
 }
 

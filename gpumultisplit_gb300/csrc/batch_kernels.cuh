@@ -238,4 +238,34 @@ __global__ void __launch_bounds__(WARP_SEG_WARPS * 32) batch_warp_kernel(const S
   }
 }
 
+// ------------------------------------------------ the batch queue
+// Records of the one-launch schedule (batch_queue.cuh runs them).
+constexpr int QUEUE_WARPS = 8;
+constexpr int QUEUE_IPT = 16;
+constexpr uint32_t QUEUE_TILE = QUEUE_WARPS * 32u * QUEUE_IPT;
+constexpr uint32_t QUEUE_PRE_TILES = 4;  // tiles per PRE item
+constexpr int QUEUE_MIN_BLOCKS = 4;                  // 64 registers: the key-value postscan's budget
+
+enum QueueItemType : uint32_t { QITEM_PRE = 0, QITEM_SCAN = 1, QITEM_POST = 2 };
+constexpr uint32_t QITEM_SHIFT = 28;
+
+// A segment as the queue sees it.  d uses the queue's layout: num_tiles of
+// QUEUE_TILE keys, matrix_off 16-byte aligned, base 0, bytes_off for every
+// identifier but delta.
+struct QSeg {
+  SegDesc d;
+  uint32_t meta;        // kind | logb << 8 | kv << 16
+  uint32_t chunks;      // scan chunks of its count matrix
+  uint32_t status_off;  // first of its chunks' look-back words
+  uint32_t pad;
+};
+
+// Device state of one run, zeroed before the launch.
+struct QueueState {
+  uint32_t* ticket;     // next item
+  uint32_t* pre_done;   // per segment: tiles counted
+  uint32_t* scan_done;  // per segment: chunks scanned
+  uint64_t* status;     // look-back words of every segment's chunks
+};
+
 }  // namespace gms

@@ -239,6 +239,26 @@ cudaError_t run_batch_warp(const BatchClassLaunch& c);
 // Dispatch on the class's kind and variant (batch.cu).
 cudaError_t run_batch_class(int kind, const BatchClassLaunch& c, int stage);
 
+struct QSeg;
+
+// The one-launch schedule of a batch (inst_queue.cu): its segment records and
+// work list, the count matrix and bucket bytes in the queue's layout, and the
+// run state (ticket, then per segment the PRE tiles and SCAN chunks done,
+// zeroed before each launch) with the chunks' look-back words.
+struct BatchQueueLaunch {
+  const QSeg* qsegs = nullptr;   // device
+  const uint2* items = nullptr;  // device
+  uint32_t num_items = 0;
+  uint32_t num_segs = 0;
+  uint32_t* matrix = nullptr;
+  uint8_t* byte_area = nullptr;
+  uint32_t* state = nullptr;     // 1 + 2 * num_segs words
+  uint64_t* status = nullptr;
+  ScratchHeader* hdr = nullptr;
+  cudaStream_t stream = nullptr;
+};
+cudaError_t run_batch_queue(const BatchQueueLaunch& c);
+
 // Creates a batch plan whose every class uses `variant` (>= 0), or the tuning
 // table's choice per segment (variant < 0).
 gms_status batch_create(const gms_segment* segments, uint32_t count, int variant, gms_batch_t* batch);

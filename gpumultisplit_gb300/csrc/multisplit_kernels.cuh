@@ -486,7 +486,10 @@ struct MatrixOffsets {
 // GIVEN: the tile's buckets were staged as bytes at the bucket-byte area (in
 // input order) by the caller, so the identifier is not evaluated; phase 3
 // overwrites that area with the buckets in sorted order.
-template <class C, class P, bool FULL, bool GIVEN = false, class Offsets = GivenOffset>
+//
+// STREAM_HINTS: the output stores mark their L2 lines evict-first (the batch
+// queue keeps keys that are read twice in L2 meanwhile; 32-bit elements).
+template <class C, class P, bool FULL, bool GIVEN = false, class Offsets = GivenOffset, bool STREAM_HINTS = false>
 __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout, typename C::VT* __restrict__ vout,
                                               uint32_t n, uint32_t cnt, Offsets& offs, const typename P::Params& bp,
                                               ScratchHeader* hdr, unsigned char* smem) {
@@ -690,6 +693,9 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
   }
 
   // ---- 4. scatter in bucket-sorted order: each bucket's run is one coalesced store
+  static_assert(!STREAM_HINTS || (C::KW == 1 && C::VW == 1), "store hints are for 32-bit elements");
+  uint64_t policy = 0;
+  if constexpr (STREAM_HINTS) policy = l2_evict_first_policy();
 #pragma unroll
   for (int j = 0; j < IPT; ++j) {
     const uint32_t p = uint32_t(j) * C::THREADS + tid;
@@ -708,8 +714,13 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
         else
           b = ident(key);
         const uint32_t g = s_delta[b] + p;
-        kout[g] = key;
-        if constexpr (C::KV) vout[g] = s_v[src];
+        if constexpr (STREAM_HINTS) {
+          st_global_hint(kout + g, key, policy);
+          if constexpr (C::KV) st_global_hint(vout + g, s_v[src], policy);
+        } else {
+          kout[g] = key;
+          if constexpr (C::KV) vout[g] = s_v[src];
+        }
       }
     }
   }
@@ -759,7 +770,11 @@ struct TileJob {
 //
 // make_offsets(job, tid, B) gives thread tid the source of bucket tid's global
 // offset (see GivenOffset); it is called while the tile's bulk copy is in flight.
-template <class C, class P, bool PREPARE = true, bool GIVEN = false, class MakeOffsets = MatrixOffsets>
+//
+// STREAM_HINTS: the tile's keys, values and bucket bytes are read, and its
+// outputs written, as evict-first L2 lines (their last use).
+template <class C, class P, bool PREPARE = true, bool GIVEN = false, class MakeOffsets = MatrixOffsets,
+          bool STREAM_HINTS = false>
 __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params, typename C::KT, typename C::VT>& job,
                                              ScratchHeader* hdr, unsigned char* smem, bool* bar_live = nullptr,
                                              MakeOffsets make_offsets = MakeOffsets()) {
@@ -795,10 +810,19 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params, t
     mbar_init(s_bar, 1);
     fence_mbar_init();
     mbar_arrive_expect_tx(s_bar, bulk * uint32_t(sizeof(KT) + (C::KV ? sizeof(VT) : 0)) + bulk_b);
-    bulk_copy_g2s(s_k, kin + base, bulk * uint32_t(sizeof(KT)), s_bar);
-    if constexpr (C::KV) bulk_copy_g2s(s_v, vin + base, bulk * uint32_t(sizeof(VT)), s_bar);
-    if constexpr (GIVEN) {
-      if (bulk_b != 0) bulk_copy_g2s(s_rb, job.bucket_bytes + base, bulk_b, s_bar);
+    if constexpr (STREAM_HINTS) {
+      const uint64_t policy = l2_evict_first_policy();
+      bulk_copy_g2s_hint(s_k, kin + base, bulk * uint32_t(sizeof(KT)), s_bar, policy);
+      if constexpr (C::KV) bulk_copy_g2s_hint(s_v, vin + base, bulk * uint32_t(sizeof(VT)), s_bar, policy);
+      if constexpr (GIVEN) {
+        if (bulk_b != 0) bulk_copy_g2s_hint(s_rb, job.bucket_bytes + base, bulk_b, s_bar, policy);
+      }
+    } else {
+      bulk_copy_g2s(s_k, kin + base, bulk * uint32_t(sizeof(KT)), s_bar);
+      if constexpr (C::KV) bulk_copy_g2s(s_v, vin + base, bulk * uint32_t(sizeof(VT)), s_bar);
+      if constexpr (GIVEN) {
+        if (bulk_b != 0) bulk_copy_g2s(s_rb, job.bucket_bytes + base, bulk_b, s_bar);
+      }
     }
     // Pull a tile that starts about one wave of blocks later into L2, so its
     // bulk copy does not wait on DRAM (only full tiles: never past the arrays).
@@ -813,7 +837,8 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params, t
     if constexpr (C::KV) s_v[i] = vin[base + i];
   }
   if constexpr (GIVEN) {
-    for (uint32_t i = bulk_b + tid; i < cnt; i += C::THREADS) s_rb[i] = job.bucket_bytes[base + i];
+    // Through L2: in the batch queue other blocks of the same launch wrote them.
+    for (uint32_t i = bulk_b + tid; i < cnt; i += C::THREADS) s_rb[i] = __ldcg(job.bucket_bytes + base + i);
   }
   if (bar_live) *bar_live = bulk != 0;
   auto offs = make_offsets(job, tid, B);
@@ -836,8 +861,10 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params, t
   }
 
   if (cnt == C::TILE)
-    return postscan_tile<C, P, true, GIVEN>(job.kout, job.vout, job.n, cnt, offs, job.bp, hdr, smem);
-  return postscan_tile<C, P, false, GIVEN>(job.kout, job.vout, job.n, cnt, offs, job.bp, hdr, smem);
+    return postscan_tile<C, P, true, GIVEN, decltype(offs), STREAM_HINTS>(job.kout, job.vout, job.n, cnt, offs,
+                                                                           job.bp, hdr, smem);
+  return postscan_tile<C, P, false, GIVEN, decltype(offs), STREAM_HINTS>(job.kout, job.vout, job.n, cnt, offs,
+                                                                          job.bp, hdr, smem);
 }
 
 // Persistent postscan over tiles first, first + stride, ... below last, for

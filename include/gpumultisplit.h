@@ -324,6 +324,25 @@ gms_status gms_batch_destroy(gms_batch_t batch);
 gms_status gms_batch_create_with_variant(const gms_segment* segments, uint32_t count, int variant,
                                          gms_batch_t* batch);
 
+/* How a run issues its work.
+ *   GMS_BATCH_SCHEDULE_CLASSES  one prescan and one postscan launch per class
+ *     of segments (same identifier kind, bucket count, key/value shape and
+ *     tile variant) and one scan per group of segments, the classes of a
+ *     stage on four side streams;
+ *   GMS_BATCH_SCHEDULE_QUEUE  one persistent launch whose blocks take work
+ *     items from a list in device memory: per segment, counting items for
+ *     groups of 4096-key tiles, scan items for its count matrix, and one
+ *     reorder item per tile.  A segment's reorder items follow its counting
+ *     items closely, so its keys are usually re-read from L2; every segment
+ *     uses 4096-key tiles (the tuning table is not consulted).
+ * Both give identical outputs.  A plan starts with GMS_BATCH_SCHEDULE_CLASSES;
+ * changing the schedule drops the plan's captured graph.  The queue needs
+ * every segment's count matrix to fit 32-bit offsets; otherwise setting it
+ * returns GMS_ERROR_NOT_SUPPORTED. */
+enum { GMS_BATCH_SCHEDULE_CLASSES = 0, GMS_BATCH_SCHEDULE_QUEUE = 1 };
+gms_status gms_batch_set_schedule(gms_batch_t batch, int schedule);
+gms_status gms_batch_get_schedule(gms_batch_t batch, int* schedule);
+
 /* -------------------------------------------------------------- tuning */
 /* The batched form runs each segment with one of GMS_NUM_TILE_VARIANTS tile
  * shapes (warps per block x keys per thread), picked from a process-wide

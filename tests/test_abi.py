@@ -5,6 +5,7 @@ import ctypes
 import re
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 import gpumultisplit_gb300 as gms
@@ -328,6 +329,59 @@ def test_batch_plan_classes_follow_the_table(gms_lib):
     h = ctypes.c_void_p()
     assert gms_lib.gms_batch_create_with_variant(arr, 1, 3, ctypes.byref(h)) == _lib.GMS_ERROR_INVALID_VALUE
     assert gms_lib.gms_batch_create_with_variant(arr, 1, -1, ctypes.byref(h)) == _lib.GMS_ERROR_INVALID_VALUE
+
+
+def test_batch_schedule_setting(gms_lib):
+    """gms_batch_set_schedule / get (host only): the queue schedule is one launch;
+    invalid schedules are refused and leave the plan's schedule unchanged."""
+    from gpumultisplit_gb300 import batched
+
+    fake = 1 << 32
+    arr = (batched.GmsSegment * 3)()
+    for i, n in enumerate((5000, 100, 70000)):
+        arr[i] = batched.GmsSegment(fake, fake, fake, fake, n, gms.delta_bucket().desc(8 << i))
+    h = ctypes.c_void_p()
+    assert gms_lib.gms_batch_create(arr, 3, ctypes.byref(h)) == 0
+    v, n = ctypes.c_int(), ctypes.c_uint32()
+    assert gms_lib.gms_batch_get_schedule(h, ctypes.byref(v)) == 0 and v.value == _lib.GMS_BATCH_SCHEDULE_CLASSES
+    assert gms_lib.gms_batch_launch_count(h, ctypes.byref(n)) == 0 and n.value > 1
+    assert gms_lib.gms_batch_set_schedule(h, _lib.GMS_BATCH_SCHEDULE_QUEUE) == 0
+    assert gms_lib.gms_batch_get_schedule(h, ctypes.byref(v)) == 0 and v.value == _lib.GMS_BATCH_SCHEDULE_QUEUE
+    assert gms_lib.gms_batch_launch_count(h, ctypes.byref(n)) == 0 and n.value == 1
+    assert gms_lib.gms_batch_set_schedule(h, 2) == _lib.GMS_ERROR_INVALID_VALUE
+    assert gms_lib.gms_batch_set_schedule(h, -1) == _lib.GMS_ERROR_INVALID_VALUE
+    assert gms_lib.gms_batch_set_schedule(None, 0) == _lib.GMS_ERROR_INVALID_VALUE
+    assert gms_lib.gms_batch_get_schedule(h, ctypes.byref(v)) == 0 and v.value == _lib.GMS_BATCH_SCHEDULE_QUEUE
+    assert gms_lib.gms_batch_set_schedule(h, _lib.GMS_BATCH_SCHEDULE_CLASSES) == 0
+    gms_lib.gms_batch_destroy(h)
+
+
+@pytest.mark.parametrize("spec", ["bench", "big_and_small"])
+def test_queue_work_list_has_no_forward_waits(gms_lib, spec):
+    """The queue's work list is built on the host and checked there: every item
+    waits only on items listed before it, else the schedule is refused.  Plans
+    over the 4096-segment batched workload and over a mix of very large and
+    tiny segments must be accepted (an ordering that put a segment's reorder
+    items between its scan items would be refused here)."""
+    from gpumultisplit_gb300 import batched, datagen
+
+    fake = 1 << 32
+    if spec == "bench":
+        sizes, buckets, kinds = datagen.batched_spec()
+    else:
+        rng = np.random.default_rng(3)
+        sizes = np.array([1 << 26, 5, 1 << 24, 4096, 3, (1 << 25) + 7] * 40, dtype=np.int64)
+        buckets = rng.choice([2, 3, 8, 100, 256], size=sizes.size)
+        kinds = ["delta" if k else "range" for k in rng.integers(0, 2, sizes.size)]
+    arr = (batched.GmsSegment * len(sizes))()
+    for i, (n, B, kind) in enumerate(zip(sizes.tolist(), buckets.tolist(), kinds)):
+        desc = (gms.delta_bucket().desc(B) if kind == "delta"
+                else _lib.BucketDesc(kind=_lib.GMS_BUCKET_RANGE, num_buckets=B, d_splitters=fake))
+        arr[i] = batched.GmsSegment(fake, fake, fake, fake, int(n), desc)
+    h = ctypes.c_void_p()
+    assert gms_lib.gms_batch_create(arr, len(sizes), ctypes.byref(h)) == 0
+    assert gms_lib.gms_batch_set_schedule(h, _lib.GMS_BATCH_SCHEDULE_QUEUE) == 0
+    gms_lib.gms_batch_destroy(h)
 
 
 def test_missing_library_fails_loudly(tmp_path):

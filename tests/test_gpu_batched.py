@@ -211,3 +211,69 @@ def test_many_tiny_segments(gms_lib, oracle_mod):
         np.testing.assert_array_equal(hko[a:b], rk)
         np.testing.assert_array_equal(hvo[a:b], rv)
     plan.close()
+
+
+# ------------------------------------------------------------ the queue schedule
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_queue_schedule_matches_oracle_mixed(gms_lib, oracle_mod, use_graph):
+    """One persistent launch over the work list: every identifier kind, power-of-two
+    and other bucket counts, key-only and key-value, empty, one-key and ragged
+    segments, each equal to the oracle."""
+    sizes = [0, 1, 7, 1024, 4095, 4096, 4097, 10000, 65537, 3, 300001, 1 << 17, 2, 99999, 32768, 33000]
+    segs, refs = make_segments(oracle_mod, sizes, 15, kinds=(0, 1, 2, 3, 4, 5),
+                               buckets=(2, 3, 4, 8, 16, 32, 64, 100, 128, 200, 256), kv_pattern=(1, 0, 1))
+    # BITS needs a power of two
+    segs = [s if not (s.identifier.desc(s.num_buckets).kind == 2 and s.num_buckets & (s.num_buckets - 1)) else None
+            for s in segs]
+    keep = [(s, r) for s, r in zip(segs, refs) if s is not None]
+    segs, refs = [s for s, _ in keep], [r for _, r in keep]
+    plan = gms.BatchedMultisplit(segs, schedule="queue")
+    assert plan.schedule == "queue" and plan.launches == 1
+    plan.run(use_graph=use_graph)
+    torch.cuda.synchronize()
+    assert plan.device_error() == 0
+    check_against_oracle(oracle_mod, segs, refs)
+    plan.close()
+
+
+def test_queue_equals_classes_and_replays(gms_lib, oracle_mod):
+    """The two schedules give the same bytes, over graph replays and after switching back and forth."""
+    rng = np.random.default_rng(17)
+    sizes = np.exp(rng.uniform(np.log(1024), np.log(1 << 18), 300)).astype(np.int64)
+    segs, refs = make_segments(oracle_mod, sizes, 17)
+    plan = gms.BatchedMultisplit(segs)
+    plan.run(use_graph=True)
+    torch.cuda.synchronize()
+    want = [(s.keys_out.clone(), s.values_out.clone()) for s in segs]
+    for schedule in ("queue", "classes", "queue"):
+        plan.schedule = schedule
+        for _ in range(2):
+            for s in segs:
+                s.keys_out.zero_()
+                s.values_out.zero_()
+            plan.run(use_graph=True)
+            torch.cuda.synchronize()
+            assert plan.device_error() == 0
+            for s, (k, v) in zip(segs, want):
+                assert torch.equal(s.keys_out, k) and torch.equal(s.values_out, v), schedule
+    check_against_oracle(oracle_mod, segs, refs)
+    plan.close()
+
+
+def test_queue_segments_longer_than_the_lag(gms_lib, oracle_mod):
+    """Segments of thousands of tiles, whose reorder items start while their own
+    counting items are still being claimed by other blocks, beside small ones;
+    skewed keys put a whole segment into one bucket."""
+    sizes = [1 << 23, 5000, (1 << 22) + 123, 1 << 12, 777]
+    segs, refs = make_segments(oracle_mod, sizes, 23, kinds=(0, 3), buckets=(2, 256), kv_pattern=(1, 0))
+    # the fourth segment: every key equal
+    s, (keys, vals, d, keep) = segs[3], refs[3]
+    keys[:] = 0x12345678
+    s.keys_in.copy_(datagen.from_u32(keys, "cuda"))
+    plan = gms.BatchedMultisplit(segs, schedule="queue")
+    for _ in range(2):
+        plan.run(use_graph=True)
+        torch.cuda.synchronize()
+        assert plan.device_error() == 0
+        check_against_oracle(oracle_mod, segs, refs)
+    plan.close()
