@@ -60,8 +60,10 @@ struct gms_batch_s {
   // which overlay the class schedule's (a run uses one schedule).
   int schedule = GMS_BATCH_SCHEDULE_CLASSES;
   bool queue_ok = false;  // the queue's count matrix fits 32-bit offsets
-  std::vector<gms::QSeg> qsegs;
-  std::vector<uint2> qitems;
+  std::vector<gms::QSeg> qsegs;     // built with the plan (one record per segment)
+  std::vector<uint2> qitems;        // built when the queue schedule is first selected
+  size_t q_items = 0;               // the list's length, known with the plan
+  void* queue_uploaded = nullptr;   // scratch that holds the queue's records and list
   size_t off_qsegs = 0, off_qitems = 0;
   size_t off_qmatrix = 0, off_qstate = 0, off_qstatus = 0, off_qbytes = 0, q_state_bytes = 0;
 };
@@ -213,17 +215,14 @@ cudaError_t launch_all(gms_batch_s* b, unsigned char* scratch, cudaStream_t s, b
 // the time its POST items are claimed and they rarely wait.
 constexpr uint32_t kQueueScanGapWaves = 2;
 
-// The queue's records and work list for the segments (the class plan's
-// descriptors give pointers, n and identifier parameters).  Segments are taken
-// class by class, largest first.  PRE items of a segment are followed by its SCAN items; the
-// list then takes the next POST tile (in segment order) whenever that
-// segment's SCAN items are far enough back and the PRE frontier leads the POST
-// frontier by GMS_QUEUE_LEAD_TILES tiles, else the next PRE or SCAN item.
+// The queue's segment records (the class plan's descriptors give pointers, n
+// and identifier parameters) and the sizes of its regions and work list.
 // Returns false when a count matrix would need offsets of 2^32 or more.
-bool build_queue(gms_batch_s* b, const gms_segment* segments, uint32_t count, uint64_t* matrix_words,
-                 uint64_t* chunks_total, uint64_t* byte_total) {
+bool queue_records(gms_batch_s* b, const gms_segment* segments, uint32_t count, uint64_t* matrix_words,
+                   uint64_t* chunks_total, uint64_t* byte_total) {
   b->qsegs.assign(count, QSeg{});
   b->qitems.clear();
+  b->q_items = 0;
   uint64_t m_total = 0, c_total = 0, bytes = 0;
   for (uint32_t i = 0; i < count; ++i) {
     const gms_segment& sg = segments[i];
@@ -246,19 +245,37 @@ bool build_queue(gms_batch_s* b, const gms_segment* segments, uint32_t count, ui
     q.status_off = uint32_t(c_total);
     c_total += q.chunks;
     q.meta = uint32_t(sg.desc.kind) | (uint32_t(logb) << 8) | (sg.d_value_in != nullptr ? 1u << 16 : 0u);
+    b->q_items += (q.d.num_tiles + QUEUE_PRE_TILES - 1) / QUEUE_PRE_TILES + q.chunks + q.d.num_tiles;
   }
+  *matrix_words = m_total;
+  *chunks_total = c_total;
+  *byte_total = bytes;
+  return true;
+}
+
+// The queue's work list over the records.  Segments are taken class by class,
+// largest first.  PRE items of a segment are followed by its SCAN items; the
+// list then takes the next POST tile (in segment order) whenever that
+// segment's last SCAN item is far enough back and the PRE frontier leads the
+// POST frontier by GMS_QUEUE_LEAD_TILES tiles, else the next PRE or SCAN item.
+// Returns false (and leaves no list) if the finished list would make an item
+// wait on a later one.
+bool build_queue_list(gms_batch_s* b) {
+  const uint32_t count = uint32_t(b->qsegs.size());
+  b->qitems.clear();
+  b->qitems.reserve(b->q_items);
   std::vector<uint32_t> order;
   for (uint32_t i = 0; i < count; ++i)
-    if (segments[i].n > 0) order.push_back(i);
+    if (b->qsegs[i].d.n > 0) order.push_back(i);
   // Segments of one class (identifier kind, bucket count, key/value) run
   // together, largest first, so the blocks running at once mostly execute
   // the same code; the classes with the most keys come first.
   std::map<uint32_t, uint64_t> class_keys;
-  for (uint32_t i : order) class_keys[b->qsegs[i].meta] += segments[i].n;
+  for (uint32_t i : order) class_keys[b->qsegs[i].meta] += b->qsegs[i].d.n;
   std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
     const uint32_t cx = b->qsegs[x].meta, cy = b->qsegs[y].meta;
     if (cx != cy) return class_keys[cx] != class_keys[cy] ? class_keys[cx] > class_keys[cy] : cx < cy;
-    return segments[x].n > segments[y].n;
+    return b->qsegs[x].d.n > b->qsegs[y].d.n;
   });
   // PRE and SCAN items in order; the POST tiles are merged in below.
   std::vector<uint2> first_stage;
@@ -309,18 +326,26 @@ bool build_queue(gms_batch_s* b, const gms_segment* segments, uint32_t count, ui
     const QSeg& q = b->qsegs[it.x];
     const uint32_t type = it.y >> QITEM_SHIFT;
     if (type == QITEM_PRE) {
-      if (scan_seen[it.x] != 0) return false;
+      if (scan_seen[it.x] != 0) {
+        b->qitems.clear();
+        return false;
+      }
       pre_seen[it.x] += std::min<uint32_t>(QUEUE_PRE_TILES, q.d.num_tiles - (it.y & ((1u << QITEM_SHIFT) - 1u)) * QUEUE_PRE_TILES);
     } else if (type == QITEM_SCAN) {
-      if (pre_seen[it.x] != q.d.num_tiles) return false;
+      if (pre_seen[it.x] != q.d.num_tiles) {
+        b->qitems.clear();
+        return false;
+      }
       ++scan_seen[it.x];
     } else if (scan_seen[it.x] != q.chunks) {
+      b->qitems.clear();
       return false;
     }
   }
-  *matrix_words = m_total;
-  *chunks_total = c_total;
-  *byte_total = bytes;
+  if (b->qitems.size() != b->q_items) {
+    b->qitems.clear();
+    return false;
+  }
   return true;
 }
 
@@ -333,7 +358,7 @@ cudaError_t launch_queue(gms_batch_s* b, unsigned char* scratch, cudaStream_t s)
   BatchQueueLaunch L;
   L.qsegs = reinterpret_cast<const QSeg*>(scratch + b->off_qsegs);
   L.items = reinterpret_cast<const uint2*>(scratch + b->off_qitems);
-  L.num_items = uint32_t(b->qitems.size());
+  L.num_items = uint32_t(b->qitems.size());  // built before the schedule could be selected
   L.num_segs = uint32_t(b->qsegs.size());
   L.matrix = reinterpret_cast<uint32_t*>(scratch + b->off_qmatrix);
   L.byte_area = scratch + b->off_qbytes;
@@ -497,15 +522,16 @@ gms_status batch_create(const gms_segment* segments, uint32_t count, int variant
     off = align_up(off + c.map_bytes(), 256);
   }
   uint64_t q_matrix = 0, q_chunks = 0, q_bytes = 0;
-  b->queue_ok = build_queue(b, segments, count, &q_matrix, &q_chunks, &q_bytes);
+  b->queue_ok = queue_records(b, segments, count, &q_matrix, &q_chunks, &q_bytes);
   if (b->queue_ok) {
     b->off_qsegs = off;
     off = align_up(off + b->qsegs.size() * sizeof(QSeg), 256);
     b->off_qitems = off;
-    off = align_up(off + b->qitems.size() * sizeof(uint2), 256);
+    off = align_up(off + b->q_items * sizeof(uint2), 256);
   } else {
     b->qsegs.clear();
-    b->qitems.clear();
+    b->q_items = 0;
+    b->off_qsegs = b->off_qitems = off;
   }
   const size_t run_start = off;  // run-time regions of either schedule start here
   b->off_matrix = off;
@@ -552,7 +578,7 @@ gms_status gms_batch_scratch_bytes(gms_batch_t batch, size_t* bytes) {
 gms_status gms_batch_launch_count(gms_batch_t batch, uint32_t* launches) {
   if (batch == nullptr || launches == nullptr) return GMS_ERROR_INVALID_VALUE;
   if (batch->schedule == GMS_BATCH_SCHEDULE_QUEUE) {
-    *launches = batch->qitems.empty() ? 0u : 1u;
+    *launches = batch->q_items == 0 ? 0u : 1u;
     return GMS_SUCCESS;
   }
   uint32_t n = 0;
@@ -567,6 +593,10 @@ gms_status gms_batch_set_schedule(gms_batch_t batch, int schedule) {
     return GMS_ERROR_INVALID_VALUE;
   if (schedule == GMS_BATCH_SCHEDULE_QUEUE && !batch->queue_ok) return GMS_ERROR_NOT_SUPPORTED;
   std::lock_guard<std::mutex> lock(batch->mu);
+  if (schedule == GMS_BATCH_SCHEDULE_QUEUE && batch->qitems.size() != batch->q_items) {
+    if (!build_queue_list(batch)) return GMS_ERROR_NOT_SUPPORTED;
+    batch->queue_uploaded = nullptr;
+  }
   if (batch->schedule != schedule) {
     // The captured graph holds the other schedule's launches.
     if (batch->exec) cudaGraphExecDestroy(batch->exec);
@@ -602,16 +632,19 @@ gms_status gms_batch_run(gms_batch_t b, void* d_scratch, size_t scratch_bytes, i
       const BatchClass& c = b->classes[i];
       e = cudaMemcpyAsync(scratch + c.map_off, c.map_data(), c.map_bytes(), cudaMemcpyHostToDevice, stream);
     }
-    if (e == cudaSuccess && b->queue_ok) {
-      e = cudaMemcpyAsync(scratch + b->off_qsegs, b->qsegs.data(), b->qsegs.size() * sizeof(QSeg),
-                          cudaMemcpyHostToDevice, stream);
-      if (e == cudaSuccess && !b->qitems.empty())
-        e = cudaMemcpyAsync(scratch + b->off_qitems, b->qitems.data(), b->qitems.size() * sizeof(uint2),
-                            cudaMemcpyHostToDevice, stream);
-    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return to_status(e);
     b->bound = d_scratch;
+  }
+  if (b->schedule == GMS_BATCH_SCHEDULE_QUEUE && b->queue_uploaded != d_scratch) {
+    e = cudaMemcpyAsync(scratch + b->off_qsegs, b->qsegs.data(), b->qsegs.size() * sizeof(QSeg),
+                        cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess && !b->qitems.empty())
+      e = cudaMemcpyAsync(scratch + b->off_qitems, b->qitems.data(), b->qitems.size() * sizeof(uint2),
+                          cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return to_status(e);
+    b->queue_uploaded = d_scratch;
   }
   e = ensure_side_streams(b);
   if (e != cudaSuccess) return to_status(e);
@@ -649,7 +682,9 @@ gms_status batch_run_async(gms_batch_t b, void* d_scratch, size_t scratch_bytes,
                            size_t pinned_bytes, cudaStream_t stream) {
   if (b == nullptr) return GMS_ERROR_INVALID_VALUE;
   if (b->classes.empty()) return GMS_SUCCESS;
-  const size_t table = batch_table_bytes(b);
+  const bool queue = b->schedule == GMS_BATCH_SCHEDULE_QUEUE;
+  // The class schedule's tables end where the queue's begin.
+  const size_t table = queue ? batch_table_bytes(b) : b->off_qsegs - b->off_segs;
   if (d_scratch == nullptr || scratch_bytes < b->bytes || h_pinned == nullptr || pinned_bytes < table)
     return GMS_ERROR_INVALID_VALUE;
   // Stage the segment table and tile maps in pinned memory at their scratch offsets, then one copy.
@@ -657,7 +692,7 @@ gms_status batch_run_async(gms_batch_t b, void* d_scratch, size_t scratch_bytes,
   std::memcpy(staging, b->segs.data(), b->segs.size() * sizeof(SegDesc));
   for (const BatchClass& c : b->classes)
     std::memcpy(staging + (c.map_off - b->off_segs), c.map_data(), c.map_bytes());
-  if (b->queue_ok) {
+  if (queue) {
     std::memcpy(staging + (b->off_qsegs - b->off_segs), b->qsegs.data(), b->qsegs.size() * sizeof(QSeg));
     std::memcpy(staging + (b->off_qitems - b->off_segs), b->qitems.data(), b->qitems.size() * sizeof(uint2));
   }
