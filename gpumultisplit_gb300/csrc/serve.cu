@@ -313,15 +313,20 @@ bool launch_round(gms_server_s* s) {
   }
   if (segs.empty() && hist_req.empty()) return false;
   // A round whose scratch does not fit while nothing else is in flight is cut
-  // in half until it does (its other requests join later rounds).
+  // in half until it does (its other requests join later rounds).  The plan
+  // that fits is the round's plan (a plan is built once per round).
   size_t keep = segs.size();
-  while (true) {
+  gms_batch_t plan = nullptr;
+  while (keep > 0) {
     size_t need = 0;
-    gms_batch_t probe = nullptr;
-    if (keep == 0 || gms_batch_create(segs.data(), uint32_t(keep), &probe) != GMS_SUCCESS) break;
-    gms_batch_scratch_bytes(probe, &need);
-    gms_batch_destroy(probe);
+    if (gms_batch_create(segs.data(), uint32_t(keep), &plan) != GMS_SUCCESS) {
+      plan = nullptr;
+      break;
+    }
+    gms_batch_scratch_bytes(plan, &need);
     if (align_up(need, kAlign) <= s->rounds_arena.size() || keep == 1) break;
+    gms_batch_destroy(plan);
+    plan = nullptr;
     keep /= 2;
   }
   if (keep < segs.size()) {
@@ -332,8 +337,7 @@ bool launch_round(gms_server_s* s) {
   Round rd;
   rd.slot = s->next_slot;
   cudaStream_t st = s->streams[rd.slot];
-  gms_batch_t plan = nullptr;
-  if (!segs.empty() && gms_batch_create(segs.data(), uint32_t(segs.size()), &plan) != GMS_SUCCESS) {
+  if (!segs.empty() && plan == nullptr) {
     for (uint64_t id : seg_req) finish(s, *s->reqs[id], GMS_ERROR_INVALID_VALUE);
     return true;
   }
