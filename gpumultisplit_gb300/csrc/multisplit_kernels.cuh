@@ -42,6 +42,13 @@
 #ifndef GMS_PAIRS_RESIDENT_THREADS
 #define GMS_PAIRS_RESIDENT_THREADS 1024
 #endif
+// Independent rank chains per warp at 65-128 buckets (1 or 2).  Two measured
+// 1.7 % faster there (1.178 against 1.198 ms for 2^28 pairs, and the 7-bit
+// sorts' passes 1.2 % faster); at 256 buckets the doubled count table and
+// tile scan made them 2.7 % slower, and at 64 they were equal.
+#ifndef GMS_RANK_CHAINS
+#define GMS_RANK_CHAINS 2
+#endif
 
 namespace gms {
 
@@ -425,7 +432,14 @@ struct PostLayout {
   static constexpr size_t R_BYTES = size_t(C::TILE) * (INDEXED ? 2 : 4);
   static constexpr size_t OFF_RB = OFF_R + R_BYTES;  // bucket bytes
   static constexpr size_t OFF_WH = (OFF_RB + (BUCKET_BYTES ? C::TILE : 0) + 15) & ~size_t(15);
-  static constexpr size_t OFF_DELTA = (OFF_WH + size_t(C::WARPS) * C::WB * C::WS * sizeof(WhT) + 15) & ~size_t(15);
+  // At 65-128 buckets a warp ranks its slots in CHAINS independent runs
+  // (slots [c*IPT/CHAINS, (c+1)*IPT/CHAINS) against count table c), so the
+  // table's read-modify-write chains of the runs interleave.  Sub-warp
+  // w*CHAINS + c holds the keys of run c of warp w, in input order.
+  static constexpr int CHAINS =
+      (C::LOGB == 7 && C::WS == 1 && GMS_PEERS_MODE == 0 && C::IPT % GMS_RANK_CHAINS == 0) ? GMS_RANK_CHAINS : 1;
+  static constexpr int SUBWARPS = C::WARPS * CHAINS;
+  static constexpr size_t OFF_DELTA = (OFF_WH + size_t(SUBWARPS) * C::WB * C::WS * sizeof(WhT) + 15) & ~size_t(15);
   static constexpr size_t OFF_SPLIT = OFF_DELTA + C::B * 4;
   // With bucket bytes from the prescan the identifier is never evaluated, so
   // it needs no shared area.
@@ -566,6 +580,30 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
         __syncwarp();
         packed[j] = (b << 16) | (v.y + rank);
       }
+    } else if constexpr (L::CHAINS == 2) {
+      // Slots j and j + IPT/2 step together, each against its own table.
+      constexpr int HALF = IPT / 2;
+      WhT* wa = s_wh + (warp * 2) * WB;
+      WhT* wb = wa + WB;
+#pragma unroll
+      for (int j = 0; j < HALF; ++j) {
+        const uint32_t pa = wbase + uint32_t(j) * 32u + lane, pb = pa + uint32_t(HALF) * 32u;
+        const bool va = FULL || pa < cnt, vb = FULL || pb < cnt;
+        const uint32_t ba = bucket_at(pa), bb = bucket_at(pb);
+        uint32_t qa = peers_by_ballot<LOGB>(ba), qb = peers_by_ballot<LOGB>(bb);
+        if (!FULL) {
+          qa &= __ballot_sync(~0u, va);
+          qb &= __ballot_sync(~0u, vb);
+        }
+        const uint32_t ra = __popc(qa & lt), rb = __popc(qb & lt);
+        const uint32_t xa = wa[ba], xb = wb[bb];
+        __syncwarp();
+        if (va && ra == 0) wa[ba] = WhT(xa + __popc(qa));
+        if (vb && rb == 0) wb[bb] = WhT(xb + __popc(qb));
+        __syncwarp();
+        packed[j] = (ba << 16) | (xa + ra);
+        packed[j + HALF] = (bb << 16) | (xb + rb);
+      }
     } else {
 #pragma unroll
       for (int j = 0; j < IPT; ++j) {
@@ -599,11 +637,12 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
     // scan and write each count-table entry once; key-only tiles, budgeted at
     // 40 registers, write the prefixes and add the start in a second pass.
     constexpr bool PREFIX_IN_REGS = C::KV;
-    uint32_t pre[PREFIX_IN_REGS ? C::WARPS : 1];
+    constexpr int SW = LOGB > 5 ? L::SUBWARPS : C::WARPS;  // count-table rows
+    uint32_t pre[PREFIX_IN_REGS ? SW : 1];
     uint32_t total = 0;
     if (tid < B) {
 #pragma unroll
-      for (int w = 0; w < C::WARPS; ++w) {
+      for (int w = 0; w < SW; ++w) {
         WhT* c_ptr = &s_wh[(w * WB + tid) * WS + (WS - 1)];
         const uint32_t c = *c_ptr;
         if constexpr (PREFIX_IN_REGS)
@@ -639,7 +678,7 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
         my_start = start;
       }
 #pragma unroll
-      for (int w = 0; w < C::WARPS; ++w) {
+      for (int w = 0; w < SW; ++w) {
         WhT* c_ptr = &s_wh[(w * WB + tid) * WS + (WS - 1)];
         if constexpr (PREFIX_IN_REGS)
           *c_ptr = WhT(pre[w] + start);
@@ -658,13 +697,15 @@ __device__ __forceinline__ bool postscan_tile(typename C::KT* __restrict__ kout,
 
   // ---- 3. bucket-sorted in-tile order (positions are a permutation of [0, cnt))
   {
-    const WhT* wh = s_wh + warp * WB * WS + (WS - 1);
+    constexpr int CH = LOGB > 5 ? L::CHAINS : 1;
+    const WhT* wh = s_wh + warp * CH * WB * WS + (WS - 1);
 #pragma unroll
     for (int j = 0; j < IPT; ++j) {
       const uint32_t pos = wbase + uint32_t(j) * 32u + lane;
       if (FULL || pos < cnt) {
         const uint32_t b = packed[j] >> 16;
-        const uint32_t d = uint32_t(wh[b * WS]) + (packed[j] & 0xFFFFu);
+        const WhT* row = wh + (j / (IPT / CH)) * WB * WS;  // the slot's chain
+        const uint32_t d = uint32_t(row[b * WS]) + (packed[j] & 0xFFFFu);
         if constexpr (L::INDEXED)
           reinterpret_cast<uint16_t*>(s_r)[d] = uint16_t(pos);
         else
@@ -845,7 +886,7 @@ __device__ __forceinline__ bool postscan_job(const TileJob<typename P::Params, t
   if constexpr (PREPARE && !GIVEN) P::prepare(s_split, job.bp);
   if constexpr (LOGB > 5) {
     // the count table as 32-bit words (its byte size is a multiple of 4)
-    constexpr uint32_t WORDS = C::WARPS * WB * C::WS * sizeof(typename L::WhT) / 4;
+    constexpr uint32_t WORDS = L::SUBWARPS * WB * C::WS * sizeof(typename L::WhT) / 4;
     for (uint32_t i = tid; i < WORDS; i += C::THREADS) s_wh[i] = 0u;
   }
   __syncthreads();
