@@ -529,6 +529,43 @@ def run_sweep(a, dev, out=None):
         return "pass" if ok else "FAIL"
 
     if a.sweep_part in ("all", "base"):
+        # The reference's CPU-runnable case (2^20 uniform keys, seed 1, 8 buckets by
+        # key >> 29, key-only): 4 MiB stays in L2, so it is a latency figure, each
+        # call timed alone (CUDA events around one call, median of 50) and checked
+        # bit for bit against the oracle.
+        n1 = 1 << 20
+        k1 = datagen.uniform_u32(n1, 1, device=dev)
+        o1 = torch.empty_like(k1)
+        ctx1 = gms.multisplit_context(8)
+        gms.multisplit_allocate_key_only(n1, ctx1)
+        call1 = lambda: gms.multisplit_key_only(k1, o1, n1, ctx1, gms.bits_bucket(29))
+        for _ in range(warm):
+            call1()
+        lat = []
+        for _ in range(50):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            call1()
+            e1.record()
+            torch.cuda.synchronize()
+            lat.append(e0.elapsed_time(e1))
+        ms1 = statistics.median(lat)
+        h1 = datagen.as_u32(k1)
+        r1, _, _ = oracle.multisplit(h1, oracle.Desc(oracle.BITS, 8, shift=29), None)
+        t0 = time.perf_counter()
+        oracle.multisplit(h1, oracle.Desc(oracle.BITS, 8, shift=29), None)
+        cpu1 = time.perf_counter() - t0
+        line1 = {"case": "multisplit k B=8 key>>29, 2^20 keys (latency, L2-resident)", "n": n1, "ms": ms1,
+                 "gkeys": n1 / (ms1 * 1e-3) / 1e9, "algorithmic_bytes_per_key": 12, "hbm_frac": None,
+                 "check": "pass" if np.array_equal(datagen.as_u32(o1), r1) else "FAIL",
+                 "cpu": {"gkeys": n1 / cpu1 / 1e9, "threads": 1, "sample_keys": n1}}
+        line1["gpu_vs_cpu"] = line1["gkeys"] / line1["cpu"]["gkeys"]
+        if out is None:
+            print(json.dumps(line1), flush=True)
+        else:
+            out.append(line1)
+        gms.multisplit_release_memory(ctx1)
+        del k1, o1
         # key-value sweep: B x distribution x identifier
         for dist in ("uniform", "zipf"):
             for ident_name in ("delta", "range"):
