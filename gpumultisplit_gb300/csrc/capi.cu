@@ -656,8 +656,7 @@ uint32_t tile_keys(int logb, bool kv) {
 cudaError_t run_scan(uint32_t* data, uint32_t m, uint64_t* status, ScratchHeader* hdr, cudaStream_t stream) {
   if (m == 0) return cudaSuccess;
   const uint32_t chunks = (m + SCAN_CHUNK - 1) / SCAN_CHUNK;
-  scan_kernel<<<chunks, SCAN_THREADS, 0, stream>>>(data, m, status, hdr);
-  return cudaGetLastError();
+  return launch_after_previous(scan_kernel, dim3(chunks), dim3(SCAN_THREADS), 0, stream, data, m, status, hdr);
 }
 
 void note_cuda_error(cudaError_t e) { g_last_cuda_error = int(e); }

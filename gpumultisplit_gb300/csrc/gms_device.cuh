@@ -158,6 +158,15 @@ __device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t* p) {
   return v;
 }
 
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization may start while the previous kernel on its stream runs;
+// griddep_wait() then blocks until that kernel has completed and its writes are
+// visible (a no-op for a kernel launched the ordinary way).
+// griddep_launch_dependents() lets the next such kernel start once every block
+// of this one has called it or exited.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
   uint32_t v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");

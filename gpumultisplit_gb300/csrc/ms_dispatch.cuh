@@ -99,9 +99,8 @@ cudaError_t launch_multisplit(const ElemT<KW>* kin, const ElemT<VW>* vin, ElemT<
       if (e != cudaSuccess) return e;
       const uint32_t wave = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
       const uint32_t dist = (GMS_PREFETCH_WAVES * wave) / 4u;
-      kern<<<g.num_tiles, C::THREADS, smem, stream>>>(kin, vin, kout, vout, n, g.num_tiles, matrix, params, hdr,
-                                                        dist, bucket_bytes);
-      return cudaGetLastError();
+      return launch_after_previous(kern, dim3(g.num_tiles), dim3(C::THREADS), smem, stream, kin, vin, kout, vout, n,
+                                   g.num_tiles, matrix, params, hdr, dist, bucket_bytes);
     }
     return cudaSuccess;
   } else {
@@ -129,9 +128,8 @@ cudaError_t launch_multisplit(const ElemT<KW>* kin, const ElemT<VW>* vin, ElemT<
       if (e != cudaSuccess) return e;
       const uint32_t wave = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
       const uint32_t dist = (GMS_PREFETCH_WAVES * wave) / 4u;
-      kern<<<g.num_tiles, C::THREADS, smem, stream>>>(kin, vin, kout, vout, n, g.num_tiles, matrix, params, hdr,
-                                                        dist, bucket_bytes);
-      return cudaGetLastError();
+      return launch_after_previous(kern, dim3(g.num_tiles), dim3(C::THREADS), smem, stream, kin, vin, kout, vout, n,
+                                   g.num_tiles, matrix, params, hdr, dist, bucket_bytes);
     }
   }
   if ((stages & STAGE_POSTSCAN) && P::USES_SMEM) {
@@ -143,8 +141,8 @@ cudaError_t launch_multisplit(const ElemT<KW>* kin, const ElemT<VW>* vin, ElemT<
     cudaError_t e = ensure_smem_limit(kern, smem, smem_done);
     if (e != cudaSuccess) return e;
     const uint32_t grid = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
-    kern<<<grid, C::THREADS, smem, stream>>>(kin, vin, kout, vout, n, g.num_tiles, matrix, params, hdr);
-    return cudaGetLastError();
+    return launch_after_previous(kern, dim3(grid), dim3(C::THREADS), smem, stream, kin, vin, kout, vout, n,
+                                 g.num_tiles, matrix, params, hdr);
   }
   if (stages & STAGE_POSTSCAN) {
     static std::atomic<uint64_t> smem_done{0};
@@ -156,9 +154,8 @@ cudaError_t launch_multisplit(const ElemT<KW>* kin, const ElemT<VW>* vin, ElemT<
     // Prefetch distance: a fraction of the number of blocks resident at once (one wave).
     const uint32_t wave = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
     const uint32_t dist = (GMS_PREFETCH_WAVES * wave) / 4u;
-    kern<<<g.num_tiles, C::THREADS, smem, stream>>>(kin, vin, kout, vout, n, g.num_tiles, matrix, params, hdr,
-                                                      dist, nullptr);
-    e = cudaGetLastError();
+    e = launch_after_previous(kern, dim3(g.num_tiles), dim3(C::THREADS), smem, stream, kin, vin, kout, vout, n,
+                              g.num_tiles, matrix, params, hdr, dist, static_cast<const uint8_t*>(nullptr));
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -399,9 +396,8 @@ cudaError_t digit_postscan_t(const DigitPass& c) {
   if (e != cudaSuccess) return e;
   const uint32_t wave = persistent_grid(kern, C::THREADS, g.num_tiles, per_sm, smem);
   const uint32_t dist = (GMS_PREFETCH_WAVES * wave) / 4u;
-  kern<<<g.num_tiles, C::THREADS, smem, c.stream>>>(c.kin, c.vin, c.kout, c.vout, c.n, g.num_tiles, matrix, c.bp,
-                                                      hdr, dist, c.bucket_bytes);
-  return cudaGetLastError();
+  return launch_after_previous(kern, dim3(g.num_tiles), dim3(C::THREADS), smem, c.stream, c.kin, c.vin, c.kout,
+                               c.vout, c.n, g.num_tiles, matrix, c.bp, hdr, dist, c.bucket_bytes);
 }
 
 #define GMS_DIGIT_SWITCH(FN, ...)                                 \

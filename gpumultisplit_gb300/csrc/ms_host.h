@@ -2,6 +2,8 @@
 // instantiation units (inst_*.cu): tile geometry, scratch layout, launchers.
 #pragma once
 
+#include <utility>
+
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -202,6 +204,26 @@ cudaError_t run_big_offsets(const uint32_t* sorted_keys, uint32_t n, const Bucke
 template <int KIND>
 cudaError_t run_histogram(const uint32_t* keys, uint32_t n, int logb, const BucketParams& bp, int32_t* hist,
                           cudaStream_t stream);
+
+// Launches `kern` on `stream` with programmatic stream serialization: its
+// blocks may be scheduled while the previous kernel on the stream finishes,
+// and they wait for it (griddep_wait) before they touch its results.  The
+// scan and the postscan of a multisplit are launched this way.
+template <class... KArgs, class... Args>
+cudaError_t launch_after_previous(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                                  Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 cudaError_t run_scan(uint32_t* data, uint32_t m, uint64_t* status, ScratchHeader* hdr, cudaStream_t stream);
 

@@ -261,6 +261,7 @@ __global__ void __launch_bounds__(C::THREADS) prescan_kernel(const uint32_t* __r
                                                              typename P::Params bp, ScratchHeader* hdr,
                                                              uint64_t* __restrict__ status, uint32_t num_chunks,
                                                              uint8_t* __restrict__ bucket_bytes) {
+  griddep_launch_dependents();  // the scan may be scheduled now; it waits for this grid
   using Counter = KeyCounter<C::LOGB, typename P::Id>;
   constexpr uint32_t G = PRESCAN_GROUP;
   __shared__ uint32_t s_hist[Counter::smem_words(C::WARPS)];
@@ -330,6 +331,7 @@ __global__ void __launch_bounds__(C::THREADS) prescan64_kernel(const uint64_t* _
                                                                typename P::Params bp, ScratchHeader* hdr,
                                                                uint64_t* __restrict__ status, uint32_t num_chunks,
                                                                uint8_t* __restrict__ bucket_bytes) {
+  griddep_launch_dependents();  // the scan may be scheduled now; it waits for this grid
   using Counter = KeyCounter<C::LOGB, typename P::Id>;
   constexpr uint32_t G = PRESCAN_GROUP;
   constexpr uint32_t TILE = C::TILE;
@@ -942,6 +944,7 @@ __global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P, GIVEN>::MIN_BLOC
     typename C::VT* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
     typename P::Params bp, ScratchHeader* hdr, uint32_t prefetch_dist, const uint8_t* __restrict__ bucket_bytes) {
   extern __shared__ __align__(128) unsigned char smem[];
+  griddep_wait();  // launched while the scan finishes: its offsets are complete past this point
   const TileJob<typename P::Params, typename C::KT, typename C::VT> job{kin,        vin,     kout, vout,
                                         n,          num_tiles, blockIdx.x, offsets,
                                         0u,         prefetch_dist != 0 ? blockIdx.x + prefetch_dist : ~0u,
@@ -959,6 +962,7 @@ __global__ void __launch_bounds__(C::THREADS, (PostLayout<C, P>::MIN_BLOCKS)) po
     typename C::VT* __restrict__ vout, uint32_t n, uint32_t num_tiles, const uint32_t* __restrict__ offsets,
     typename P::Params bp, ScratchHeader* hdr) {
   extern __shared__ __align__(128) unsigned char smem[];
+  griddep_wait();  // launched while the scan finishes: its offsets are complete past this point
   postscan_run<C, P>(
       blockIdx.x, num_tiles, gridDim.x,
       [&](uint32_t t, uint32_t prefetch) {

@@ -15,6 +15,8 @@ namespace gms {
 __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(uint32_t* __restrict__ data, uint32_t m,
                                                             uint64_t* __restrict__ status, ScratchHeader* hdr) {
   __shared__ uint32_t s_chunk;
+  griddep_wait();  // launched while the prescan finishes: the counts and the reset ticket are in place
+  griddep_launch_dependents();
   if (threadIdx.x == 0) s_chunk = atomicAdd(&hdr->ticket, 1u);
   __syncthreads();
   const uint32_t chunk = s_chunk;
